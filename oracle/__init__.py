@@ -1,0 +1,221 @@
+"""Oracle (test infrastructure only).
+
+ctypes binding of the plain-C restatement in ``oracle/spk_oracle.c`` and the
+recipe that builds it.  Only the tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import this package; the product path
+(``spparks_gb300``) never does.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "libspkoracle.so"
+
+LATTICES = {"sq/4n": 0, "sq/8n": 1, "sc/6n": 2, "sc/26n": 3}
+APPS = {"ising": 0, "potts": 1, "potts/neighonly": 2, "potts/neigh": 3}
+RNG_PHILOX, RNG_STRICT = 0, 1
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle restatement into ``oracle/_build``."""
+    src = HERE / "spk_oracle.c"
+    deps = [src, HERE / "spk_oracle.h", HERE / "philox_oracle.h"]
+    if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    tmp = BUILD / f"libspkoracle.{os.getpid()}.so"
+    subprocess.check_call(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-o", str(tmp), str(src), "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_reference(jobs: int = 8) -> bool:
+    """Build the reference (and its Philox-shim variant) into ``oracle/_ref``
+    when the reference sources are present; returns False when they are not."""
+    ref = os.environ.get("SPK_REFERENCE_SRC", "/root/reference/src")
+    if not Path(ref, "app_lattice.cpp").exists():
+        return False
+    subprocess.check_call(["make", "-s", "-C", str(HERE / "ref"), f"-j{jobs}", f"REF={ref}"])
+    return True
+
+
+class Cfg(ctypes.Structure):
+    _fields_ = [
+        ("lattice", ctypes.c_int),
+        ("nx", ctypes.c_int),
+        ("ny", ctypes.c_int),
+        ("nz", ctypes.c_int),
+        ("app", ctypes.c_int),
+        ("nspins", ctypes.c_int),
+        ("temperature", ctypes.c_double),
+        ("nsector", ctypes.c_int),
+        ("nloop", ctypes.c_int),
+        ("rng", ctypes.c_int),
+        ("seed", ctypes.c_uint32),
+        ("mask", ctypes.c_int),
+        ("px", ctypes.c_int),
+        ("py", ctypes.c_int),
+        ("pz", ctypes.c_int),
+    ]
+
+
+class RanMars(ctypes.Structure):
+    _fields_ = [
+        ("u", ctypes.c_double * 98),
+        ("c", ctypes.c_double),
+        ("cd", ctypes.c_double),
+        ("cm", ctypes.c_double),
+        ("i97", ctypes.c_int),
+        ("j97", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB))
+        P = ctypes.POINTER
+        i32p, i64p, u64p, u8p, dblp = (P(ctypes.c_int32), P(ctypes.c_int64), P(ctypes.c_uint64),
+                                       P(ctypes.c_uint8), P(ctypes.c_double))
+        L.spko_philox.argtypes = [P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_uint32)]
+        L.spko_neighbors.argtypes = [P(Cfg), ctypes.c_int64, i64p]
+        L.spko_neighbors.restype = ctypes.c_int
+        L.spko_color.argtypes = [P(Cfg), ctypes.c_int64]
+        L.spko_sector.argtypes = [P(Cfg), ctypes.c_int64]
+        L.spko_energy.argtypes = [P(Cfg), i32p]
+        L.spko_energy.restype = ctypes.c_double
+        L.spko_hash.argtypes = [i32p, ctypes.c_int64]
+        L.spko_hash.restype = ctypes.c_uint64
+        L.spko_init_spins.argtypes = [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int, ctypes.c_int, i32p]
+        L.spko_color_sweeps.argtypes = [P(Cfg), i32p, ctypes.c_int64, ctypes.c_int, i64p, i64p, u64p,
+                                        i32p, u8p]
+        L.spko_color_sweeps.restype = ctypes.c_int
+        L.spko_ranmars_init.argtypes = [P(RanMars), ctypes.c_int]
+        L.spko_ranmars_uniform.argtypes = [P(RanMars)]
+        L.spko_ranmars_uniform.restype = ctypes.c_double
+        L.spko_park_uniform.argtypes = [i32p]
+        L.spko_park_uniform.restype = ctypes.c_double
+        L.spko_park_seed_from_double.argtypes = [ctypes.c_double]
+        L.spko_park_seed_from_double.restype = ctypes.c_int32
+        L.spko_park_reset.argtypes = [ctypes.c_double, ctypes.c_int64, ctypes.c_int]
+        L.spko_park_reset.restype = ctypes.c_int32
+        L.spko_set_range.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_int, ctypes.c_int, i32p]
+        L.spko_random_sector_sweeps.argtypes = [P(Cfg), i32p, i32p, ctypes.c_int, i64p, i64p]
+        L.spko_kmc_create.argtypes = [P(Cfg), ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.spko_kmc_create.restype = ctypes.c_void_p
+        L.spko_kmc_destroy.argtypes = [ctypes.c_void_p]
+        L.spko_kmc_run.argtypes = [ctypes.c_void_p, i32p, dblp, ctypes.c_double, i64p, u64p, dblp,
+                                   ctypes.c_int]
+        L.spko_kmc_run.restype = ctypes.c_int
+        L.spko_kmc_total_propensity.argtypes = [ctypes.c_void_p]
+        L.spko_kmc_total_propensity.restype = ctypes.c_double
+        L.spko_kmc_nchains.argtypes = [ctypes.c_void_p]
+        L.spko_kmc_chain_events.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.spko_kmc_chain_events.restype = ctypes.c_uint64
+        _lib = L
+    return _lib
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def make_cfg(lattice="sq/4n", nx=8, ny=8, nz=1, app="ising", nspins=2, temperature=0.0, nsector=1,
+             nloop=1, rng=RNG_PHILOX, seed=1, mask=0, procs=(1, 1, 1)) -> Cfg:
+    return Cfg(LATTICES[lattice], nx, ny, nz, APPS[app], nspins, float(temperature), nsector, nloop, rng,
+               seed & 0xFFFFFFFF, int(mask), procs[0], procs[1], procs[2])
+
+
+def philox(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib().spko_philox(c, k, o)
+    return list(o)
+
+
+def nsites(cfg: Cfg) -> int:
+    return cfg.nx * cfg.ny * cfg.nz
+
+
+def init_spins(seed: int, n: int, lo: int, hi: int) -> np.ndarray:
+    s = np.empty(n, dtype=np.int32)
+    lib().spko_init_spins(seed & 0xFFFFFFFF, n, lo, hi, _ptr(s, ctypes.c_int32))
+    return s
+
+
+def neighbors(cfg: Cfg, i: int) -> list[int]:
+    out = (ctypes.c_int64 * 26)()
+    n = lib().spko_neighbors(ctypes.byref(cfg), i, out)
+    return list(out[:n])
+
+
+def color_sweeps(cfg: Cfg, spin: np.ndarray, sweep0: int, nsweeps: int, siteseeds=None, mask=None):
+    """Runs nsweeps colour sweeps in place; returns (naccept, nattempt, hashes)."""
+    assert spin.dtype == np.int32 and spin.flags.c_contiguous
+    na = ctypes.c_int64(0)
+    nt = ctypes.c_int64(0)
+    hashes = np.zeros(max(nsweeps, 1), dtype=np.uint64)
+    ss = _ptr(siteseeds, ctypes.c_int32) if siteseeds is not None else None
+    mk = _ptr(mask, ctypes.c_uint8) if mask is not None else None
+    rc = lib().spko_color_sweeps(ctypes.byref(cfg), _ptr(spin, ctypes.c_int32), sweep0, nsweeps,
+                                 ctypes.byref(na), ctypes.byref(nt), _ptr(hashes, ctypes.c_uint64), ss, mk)
+    if rc != 0:
+        raise RuntimeError(f"oracle colour sweep failed: {rc}")
+    return na.value, nt.value, hashes[:nsweeps]
+
+
+def energy(cfg: Cfg, spin: np.ndarray) -> float:
+    return lib().spko_energy(ctypes.byref(cfg), _ptr(spin, ctypes.c_int32))
+
+
+def spin_hash(spin: np.ndarray) -> int:
+    s = np.ascontiguousarray(spin, dtype=np.int32)
+    return int(lib().spko_hash(_ptr(s, ctypes.c_int32), s.size))
+
+
+class Kmc:
+    """Tree-solver KMC over sectors (and an optional processor grid)."""
+
+    def __init__(self, cfg: Cfg, nstop: float = 1.0, tstop: float = 0.0):
+        self.cfg = cfg
+        self.h = lib().spko_kmc_create(ctypes.byref(cfg), 1 if tstop <= 0 else 0, nstop, tstop)
+        self.time = 0.0
+        self.naccept = 0
+
+    def run(self, spin: np.ndarray, dt: float, maxrec: int = 100000):
+        t = ctypes.c_double(self.time)
+        na = ctypes.c_int64(self.naccept)
+        hashes = np.zeros(maxrec, dtype=np.uint64)
+        times = np.zeros(maxrec, dtype=np.float64)
+        npass = lib().spko_kmc_run(self.h, _ptr(spin, ctypes.c_int32), ctypes.byref(t), self.time + dt,
+                                   ctypes.byref(na), _ptr(hashes, ctypes.c_uint64), _ptr(times, ctypes.c_double),
+                                   maxrec)
+        self.time = t.value
+        self.naccept = na.value
+        k = min(npass, maxrec)
+        return npass, hashes[:k], times[:k]
+
+    def total_propensity(self) -> float:
+        return lib().spko_kmc_total_propensity(self.h)
+
+    def chain_events(self) -> list[int]:
+        n = lib().spko_kmc_nchains(self.h)
+        return [int(lib().spko_kmc_chain_events(self.h, c)) for c in range(n)]
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().spko_kmc_destroy(self.h)
+            self.h = None

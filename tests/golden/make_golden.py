@@ -1,0 +1,223 @@
+"""Generate the golden parity fixtures from the reference itself.
+
+Runs the reference SPPARKS built from its own sources by ``oracle/ref/Makefile``
+(``oracle/_ref/runner_philox``: stock apps and tree solver with a Philox
+RandomPark shim; ``oracle/_ref/runner_plain`` and ``spk_serial``: unmodified)
+on small cases and writes ``tests/golden/*.json``.  It also copies the
+Naccept/Nreject/Energy columns of the reference's example logs
+(examples/ising, examples/potts), which are the reference's own golden
+vectors for its rejection path.
+
+Usage (needs the reference sources; not run by the tests):
+    python tests/golden/make_golden.py [--ref /path/to/spparks]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+DT_SWEEP = {"ising": lambda q, z: 0.5, "potts": lambda q, z: 1.0 / q,
+            "potts/neighonly": lambda q, z: 1.0 / z, "potts/neigh": lambda q, z: 1.0 / z}
+MAXNEIGH = {"sq/4n": 4, "sq/8n": 8, "sc/6n": 6, "sc/26n": 26}
+
+
+def geometry_lines(lattice, nx, ny, nz):
+    if lattice.startswith("sq"):
+        return ["dimension 2", f"lattice {lattice} 1.0", f"region box block 0 {nx} 0 {ny} -0.5 0.5",
+                "create_box box", "create_sites box"]
+    return ["dimension 3", f"lattice {lattice} 1.0", f"region box block 0 {nx} 0 {ny} 0 {nz}",
+            "create_box box", "create_sites box"]
+
+
+def app_line(app, q):
+    return "app_style ising" if app == "ising" else f"app_style {app} {q}"
+
+
+def run_time(case):
+    """A run time that yields exactly case['nsweeps'] passes whatever the
+    rounding of dt_sweep: stop half a sweep before the last one ends."""
+    dt = DT_SWEEP[case["app"]](case["nspins"], MAXNEIGH[case["lattice"]])
+    nloop = case.get("nloop", 1)
+    return (case["nsweeps"] - 0.5) * dt * nloop
+
+
+def sweep_script(case):
+    c = case
+    lines = ["seed 56789", app_line(c["app"], c["nspins"])]
+    lines += geometry_lines(c["lattice"], c["nx"], c["ny"], c["nz"])
+    lines += [f"#! seed {c['seed']}", f"#! init_spins 1 {c['nspins']}", "#! snap init"]
+    lines.append("sweep color" + (" mask yes" if c.get("mask") else ""))
+    if c.get("nsector", 1) > 1:
+        s = "sector yes" if c["nsector"] in (4, 8) and not c.get("nsector_explicit") else f"sector {c['nsector']}"
+        if c.get("nloop", 1) > 1:
+            s += f" nstop {c['nloop']}"
+        lines.append(s)
+    lines.append(f"temperature {c['temperature']!r}")
+    lines += ["#! record on", f"run {run_time(c)!r}", "#! snap final"]
+    return lines
+
+
+def kmc_script(case):
+    c = case
+    lines = ["seed 56789", app_line(c["app"], c["nspins"])]
+    lines += geometry_lines(c["lattice"], c["nx"], c["ny"], c["nz"])
+    lines += [f"#! seed {c['seed']}", f"#! init_spins 1 {c['nspins']}", "#! snap init",
+              "solve_style tree", "sector yes", f"temperature {c['temperature']!r}", "#! record on"]
+    for k, t in enumerate(c["runs"]):
+        lines += [f"run {t!r}", f"#! snap run{k}"]
+    return lines
+
+
+def strict_script(case):
+    c = case
+    lines = ["seed %d" % c["master_seed"], app_line(c["app"], c["nspins"])]
+    lines += geometry_lines(c["lattice"], c["nx"], c["ny"], c["nz"])
+    lines += [f"set site range 1 {c['nspins']}", "#! snap init", "sweep color/strict",
+              f"temperature {c['temperature']!r}"]
+    dt = DT_SWEEP[c["app"]](c["nspins"], MAXNEIGH[c["lattice"]])
+    for k in range(c["nruns"]):
+        lines += [f"run {(c['sweeps_per_run'] - 0.5) * dt!r}", f"#! snap run{k}", "#! energy"]
+    return lines
+
+
+def parse_output(text):
+    out = {"sweeps": [], "snaps": {}, "energies": []}
+    for line in text.splitlines():
+        p = line.split()
+        if not p:
+            continue
+        if p[0] == "sweep":
+            out["sweeps"].append([int(p[1]), int(p[2]), int(p[3]), p[4], float(p[5])])
+        elif p[0] == "snap":
+            n = int(p[3])
+            out["snaps"][p[1]] = {"hash": p[2], "spins": [int(v) for v in p[4:4 + n]]}
+        elif p[0] == "energy":
+            out["energies"].append(float(p[1]))
+    return out
+
+
+def run_runner(binary, lines):
+    with tempfile.NamedTemporaryFile("w", suffix=".in", delete=False, dir=str(ROOT / "oracle" / "_ref")) as f:
+        f.write("\n".join(lines) + "\n")
+        path = f.name
+    try:
+        res = subprocess.run([str(binary), path], capture_output=True, text=True, check=True,
+                             cwd=str(ROOT / "oracle" / "_ref"))
+    finally:
+        os.unlink(path)
+    return parse_output(res.stdout)
+
+
+SWEEP_CASES = [
+    dict(name="ising_sq4n_16_T2269", app="ising", nspins=2, lattice="sq/4n", nx=16, ny=16, nz=1,
+         temperature=2.269, seed=56789, nsweeps=12),
+    dict(name="ising_sq4n_16_T0", app="ising", nspins=2, lattice="sq/4n", nx=16, ny=12, nz=1,
+         temperature=0.0, seed=11, nsweeps=6),
+    dict(name="ising_sc6n_8_T22557", app="ising", nspins=2, lattice="sc/6n", nx=8, ny=6, nz=4,
+         temperature=2.2557, seed=99, nsweeps=6),
+    dict(name="potts_sq8n_16_Q8", app="potts", nspins=8, lattice="sq/8n", nx=16, ny=16, nz=1,
+         temperature=1.0, seed=7, nsweeps=8),
+    dict(name="potts_sc26n_8_Q100", app="potts", nspins=100, lattice="sc/26n", nx=8, ny=8, nz=8,
+         temperature=0.5, seed=5, nsweeps=4),
+    dict(name="neighonly_sc26n_8_Q100", app="potts/neighonly", nspins=100, lattice="sc/26n", nx=8, ny=8,
+         nz=8, temperature=0.5, seed=56789, nsweeps=6),
+    dict(name="neighonly_sq8n_12_Q5", app="potts/neighonly", nspins=5, lattice="sq/8n", nx=12, ny=8,
+         nz=1, temperature=0.3, seed=3, nsweeps=10),
+    dict(name="neigh_sq4n_16_Q20", app="potts/neigh", nspins=20, lattice="sq/4n", nx=16, ny=16, nz=1,
+         temperature=0.8, seed=21, nsweeps=8),
+    dict(name="potts_sq4n_sector4_Q16", app="potts", nspins=16, lattice="sq/4n", nx=16, ny=16, nz=1,
+         temperature=0.7, seed=4, nsweeps=5, nsector=4),
+    dict(name="ising_sc26n_sector8", app="ising", nspins=2, lattice="sc/26n", nx=8, ny=8, nz=8,
+         temperature=3.0, seed=8, nsweeps=3, nsector=8),
+    dict(name="neighonly_sq4n_sector2_nstop2", app="potts/neighonly", nspins=10, lattice="sq/4n", nx=12,
+         ny=8, nz=1, temperature=0.6, seed=12, nsweeps=4, nsector=2, nsector_explicit=True, nloop=2),
+    dict(name="potts_sq4n_mask_sector4_T0", app="potts", nspins=4, lattice="sq/4n", nx=16, ny=16, nz=1,
+         temperature=0.0, seed=13, nsweeps=6, nsector=4, mask=True),
+    dict(name="ising_sq4n_mask_T1", app="ising", nspins=2, lattice="sq/4n", nx=8, ny=8, nz=1,
+         temperature=1.0, seed=14, nsweeps=4, mask=True),
+]
+
+KMC_CASES = [
+    dict(name="kmc_potts_sq8n_16_Q10", app="potts", nspins=10, lattice="sq/8n", nx=16, ny=16, nz=1,
+         temperature=1.0, seed=31, runs=[1.5, 0.75]),
+    dict(name="kmc_ising_sq4n_16", app="ising", nspins=2, lattice="sq/4n", nx=16, ny=16, nz=1,
+         temperature=2.0, seed=32, runs=[2.0]),
+    dict(name="kmc_potts_sc26n_8_Q50", app="potts", nspins=50, lattice="sc/26n", nx=8, ny=8, nz=8,
+         temperature=0.8, seed=33, runs=[0.6]),
+]
+
+STRICT_CASES = [
+    dict(name="strict_ising_sq4n_16", app="ising", nspins=2, lattice="sq/4n", nx=16, ny=16, nz=1,
+         temperature=2.269, master_seed=56789, nruns=3, sweeps_per_run=4),
+    dict(name="strict_neighonly_sc26n_6", app="potts/neighonly", nspins=100, lattice="sc/26n", nx=6,
+         ny=6, nz=6, temperature=0.5, master_seed=4321, nruns=2, sweeps_per_run=3),
+    dict(name="strict_potts_sq8n_12_Q4", app="potts", nspins=4, lattice="sq/8n", nx=12, ny=12, nz=1,
+         temperature=0.9, master_seed=777, nruns=2, sweeps_per_run=5),
+]
+
+
+def example_log_rows(path):
+    rows = []
+    lines = Path(path).read_text().splitlines()
+    for k, line in enumerate(lines):
+        if line.split()[:4] == ["Time", "Naccept", "Nreject", "Nsweeps"]:
+            for row in lines[k + 1:]:
+                p = row.split()
+                if len(p) != 6:
+                    break
+                rows.append({"time": float(p[0]), "naccept": int(p[1]), "nreject": int(p[2]),
+                             "nsweeps": int(p[3]), "energy": float(p[5])})
+            break
+    return rows
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    refsrc = Path(args.ref) / "src"
+    subprocess.check_call(["make", "-s", "-C", str(ROOT / "oracle" / "ref"), "-j8", f"REF={refsrc}"])
+    philox = ROOT / "oracle" / "_ref" / "runner_philox"
+    plain = ROOT / "oracle" / "_ref" / "runner_plain"
+
+    fixtures = {"sweeps": [], "kmc": [], "strict": []}
+    for case in SWEEP_CASES:
+        lines = sweep_script(case)
+        res = run_runner(philox, lines)
+        assert len(res["sweeps"]) == case["nsweeps"], (case["name"], len(res["sweeps"]))
+        fixtures["sweeps"].append({"case": case, "script": lines, **res})
+        print("sweep case", case["name"], "final", res["snaps"]["final"]["hash"])
+    for case in KMC_CASES:
+        lines = kmc_script(case)
+        res = run_runner(philox, lines)
+        fixtures["kmc"].append({"case": case, "script": lines, **res})
+        print("kmc case", case["name"], "passes", len(res["sweeps"]))
+    for case in STRICT_CASES:
+        lines = strict_script(case)
+        res = run_runner(plain, lines)
+        fixtures["strict"].append({"case": case, "script": lines, **res})
+        print("strict case", case["name"], [res["snaps"][f"run{k}"]["hash"] for k in range(case["nruns"])])
+
+    (HERE / "reference_philox.json").write_text(json.dumps(fixtures, indent=1))
+    logs = {
+        "ising": {"script": (Path(args.ref) / "examples/ising/in.ising").read_text().splitlines(),
+                  "rows": example_log_rows(Path(args.ref) / "examples/ising/log.ising.11Nov09.linux.1")},
+        "potts": {"script": (Path(args.ref) / "examples/potts/in.potts").read_text().splitlines(),
+                  "rows": example_log_rows(Path(args.ref) / "examples/potts/log.potts.11Nov09.linux.1")},
+    }
+    (HERE / "example_logs.json").write_text(json.dumps(logs, indent=1))
+    print("wrote", HERE / "reference_philox.json", HERE / "example_logs.json")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,150 @@
+"""Pins the oracle restatement (oracle/spk_oracle.c) before it is trusted as
+the GPU path's checker: against the published Philox known-answer vectors,
+the reference's own example logs, and fixtures produced by the reference
+itself (tests/golden/make_golden.py)."""
+
+import numpy as np
+import pytest
+
+import oracle
+
+# Philox4x32-10 known-answer vectors published with the Random123 library
+PHILOX_KAT = [
+    ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+    ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+    ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+     [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+]
+
+
+@pytest.mark.parametrize("ctr,key,expect", PHILOX_KAT)
+def test_philox_known_answers(ctr, key, expect):
+    assert oracle.philox(ctr, key) == expect
+
+
+def cfg_from_case(case, rng=oracle.RNG_PHILOX, seed=None):
+    return oracle.make_cfg(case["lattice"], case["nx"], case["ny"], case["nz"], case["app"], case["nspins"],
+                           case["temperature"], case.get("nsector", 1), case.get("nloop", 1), rng,
+                           case.get("seed", 0) if seed is None else seed, case.get("mask", False))
+
+
+def test_neighbor_order_matches_reference_offsets():
+    # CreateSites::offsets_2d/3d order: dx outer, dy, dz inner
+    c = oracle.make_cfg("sq/4n", 8, 8)
+    i = 3 + 8 * 4
+    assert oracle.neighbors(c, i) == [2 + 32, 3 + 24, 3 + 40, 4 + 32]
+    c6 = oracle.make_cfg("sc/6n", 4, 4, 4)
+    i = 1 + 4 * (1 + 4 * 1)
+    x, y, z = 1, 1, 1
+    idx = lambda a, b, d: a + 4 * (b + 4 * d)
+    assert oracle.neighbors(c6, i) == [idx(0, 1, 1), idx(1, 0, 1), idx(1, 1, 0), idx(1, 1, 2), idx(1, 2, 1),
+                                       idx(2, 1, 1)]
+    c26 = oracle.make_cfg("sc/26n", 4, 4, 4)
+    nb = oracle.neighbors(c26, 0)
+    assert len(nb) == 26 and nb[0] == idx(3, 3, 3) and nb[-1] == idx(1, 1, 1)
+
+
+@pytest.mark.parametrize("k", range(13))
+def test_sweeps_match_reference(ref_fixtures, k):
+    fx = ref_fixtures["sweeps"][k]
+    case = fx["case"]
+    cfg = cfg_from_case(case)
+    spin = np.array(fx["snaps"]["init"]["spins"], dtype=np.int32)
+    assert spin.tolist() == oracle.init_spins(case["seed"], spin.size, 1, case["nspins"]).tolist()
+    mask = np.zeros(spin.size, dtype=np.uint8) if case.get("mask") else None
+    na, nt, hashes = oracle.color_sweeps(cfg, spin, 0, case["nsweeps"], mask=mask)
+    ref = fx["sweeps"]
+    assert [format(int(h), "016x") for h in hashes] == [r[3] for r in ref]
+    assert na == ref[-1][1] and nt == ref[-1][2]
+    assert spin.tolist() == fx["snaps"]["final"]["spins"]
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_kmc_matches_reference(ref_fixtures, k):
+    fx = ref_fixtures["kmc"][k]
+    case = fx["case"]
+    cfg = cfg_from_case(case)
+    cfg.nsector = 4 if case["lattice"].startswith("sq") else 8
+    spin = np.array(fx["snaps"]["init"]["spins"], dtype=np.int32)
+    km = oracle.Kmc(cfg)
+    recs = []
+    for r, t in enumerate(case["runs"]):
+        npass, hashes, times = km.run(spin, t)
+        recs += [(format(int(h), "016x"), float(tm)) for h, tm in zip(hashes, times)]
+        assert spin.tolist() == fx["snaps"][f"run{r}"]["spins"]
+    ref = fx["sweeps"]
+    assert [h for h, _ in recs] == [r[3] for r in ref]
+    for (_, tm), r in zip(recs, ref):
+        assert tm == pytest.approx(r[4], rel=1e-12)
+    assert km.naccept == ref[-1][1]
+
+
+def ranmars_draws(seed, n):
+    r = oracle.RanMars()
+    oracle.lib().spko_ranmars_init(oracle.ctypes.byref(r), seed)
+    return [oracle.lib().spko_ranmars_uniform(oracle.ctypes.byref(r)) for _ in range(n)]
+
+
+def park_seed(d):
+    return oracle.lib().spko_park_seed_from_double(d)
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_strict_matches_unmodified_reference(ref_fixtures, k):
+    """sweep color/strict with the reference's own RanMars/Park-Miller seeding:
+    ranmaster draw 1 -> set site range, 2-3 -> ranapp, 4-5 -> ranstrict and the
+    per-site seeds (src/app_lattice.cpp:274-295, src/set.cpp:598-624)."""
+    fx = ref_fixtures["strict"][k]
+    case = fx["case"]
+    cfg = cfg_from_case(case, rng=oracle.RNG_STRICT, seed=0)
+    n = case["nx"] * case["ny"] * case["nz"]
+    u = ranmars_draws(case["master_seed"], 5)
+    spin = np.empty(n, dtype=np.int32)
+    oracle.lib().spko_set_range(park_seed(u[0]), n, 1, case["nspins"], oracle._ptr(spin, oracle.ctypes.c_int32))
+    assert spin.tolist() == fx["snaps"]["init"]["spins"]
+    seeds = np.array([oracle.lib().spko_park_reset(u[4], i + 1, 100) for i in range(n)], dtype=np.int32)
+    sweep = 0
+    for r in range(case["nruns"]):
+        oracle.color_sweeps(cfg, spin, sweep, case["sweeps_per_run"], siteseeds=seeds)
+        sweep += case["sweeps_per_run"]
+        assert spin.tolist() == fx["snaps"][f"run{r}"]["spins"]
+        assert oracle.energy(cfg, spin) == fx["energies"][r]
+
+
+def example_run(example_logs, which, rows):
+    """Reproduces the reference example (sweep random + sector yes, T=0) with the
+    oracle's RanMars/Park-Miller restatement: ranmaster draw 1 -> set site range,
+    draws 2-3 -> ranapp (src/app_lattice.cpp:274-278)."""
+    if which == "ising":
+        cfg = oracle.make_cfg("sq/4n", 50, 50, 1, "ising", 2, 0.0, nsector=4)
+        q = 2
+    else:
+        cfg = oracle.make_cfg("sc/26n", 20, 20, 20, "potts", 100, 0.0, nsector=8)
+        q = 100
+    n = oracle.nsites(cfg)
+    u = ranmars_draws(56789, 3)
+    spin = np.empty(n, dtype=np.int32)
+    oracle.lib().spko_set_range(park_seed(u[0]), n, 1, q, oracle._ptr(spin, oracle.ctypes.c_int32))
+    ranapp = np.array([oracle.lib().spko_park_reset(u[2], 0, 100)], dtype=np.int32)
+    ranapp[0] = oracle.lib().spko_park_reset(u[2], 0, 100)
+    # RandomPark(u[1]) is overwritten by reset(u[2], me=0, 100)
+    log = example_logs[which]["rows"]
+    assert oracle.energy(cfg, spin) == log[0]["energy"]
+    done = 0
+    na = oracle.ctypes.c_int64(0)
+    nt = oracle.ctypes.c_int64(0)
+    for row in log[1:rows + 1]:
+        oracle.lib().spko_random_sector_sweeps(oracle.ctypes.byref(cfg), oracle._ptr(spin, oracle.ctypes.c_int32),
+                                               oracle._ptr(ranapp, oracle.ctypes.c_int32), row["nsweeps"] - done,
+                                               oracle.ctypes.byref(na), oracle.ctypes.byref(nt))
+        done = row["nsweeps"]
+        assert (na.value, nt.value - na.value) == (row["naccept"], row["nreject"])
+        assert oracle.energy(cfg, spin) == row["energy"]
+
+
+def test_example_log_ising(example_logs):
+    example_run(example_logs, "ising", 10)
+
+
+def test_example_log_potts(example_logs):
+    example_run(example_logs, "potts", 2)
