@@ -1,0 +1,146 @@
+/* spkgpu: GB300-native (sm_103a) on-lattice Monte Carlo hot path of SPPARKS.
+
+   A plain C ABI (pointers, sizes, status codes) over hand-written CUDA
+   kernels.  It replaces, for one lattice on one GPU, the per-site virtual
+   calls that AppLattice makes on the host:
+
+     spkgpu_sweep        AppLattice::iterate_rejection with `sweep color` or
+                         `sweep color/strict` (src/app_lattice.cpp:632-711)
+                         calling AppIsing/AppPotts/AppPottsNeighOnly/
+                         AppPottsNeigh::site_event_rejection
+                         (src/app_ising.cpp:104-136, src/app_potts.cpp:112-146,
+                         src/app_potts_neighonly.cpp:71-117,
+                         src/app_potts_neigh.cpp:71-116)
+     spkgpu_kmc_run      AppLattice::iterate_kmc_sector with `solve_style tree`
+                         (src/app_lattice.cpp:517-626, src/solve_tree.cpp:109-224,
+                         src/app_potts.cpp:153-244, src/app_ising.cpp:143-196)
+     spkgpu_energy       spparks_energy / DiagEnergy (src/library.cpp:118-147,
+                         src/diag_energy.cpp:53-68)
+     spkgpu_upload_spins / spkgpu_download_spins
+                         the host<->device sync of App::iarray[0] that a host
+                         AppLattice subclass performs around iterate()
+                         (src/app.cpp:179-182)
+
+   Every entry point returns 0 on success or a negative SPKGPU_ERR_* code and
+   never exits the process; spkgpu_last_error() returns the message of the
+   last failure on a handle.  A handle owns one CUDA stream; calls on one
+   handle must come from one host thread at a time.
+
+   Random numbers: Philox4x32-10 keyed by (seed, stream) with counter
+   (site pair, sweep, pass), as stated in spparks_gb300/csrc/spk_philox.cuh.  With
+   SPKGPU_RNG_STRICT each site carries the reference's own Park-Miller state
+   (sweep color/strict, src/app_lattice.cpp:287-295, 796-805) instead. */
+#ifndef SPKGPU_H
+#define SPKGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPKGPU_OK 0
+#define SPKGPU_ERR_ARG (-1)         /* invalid argument or configuration */
+#define SPKGPU_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define SPKGPU_ERR_STATE (-3)       /* call not valid in the handle's state */
+#define SPKGPU_ERR_NOMEM (-4)       /* device allocation failed */
+#define SPKGPU_ERR_UNSUPPORTED (-5) /* combination not implemented */
+#define SPKGPU_ERR_INVALID_SPIN (-6) /* a site value is outside 1..nspins */
+
+/* lattice styles (src/lattice.cpp:43-57); periodic boxes only */
+#define SPKGPU_SQ_4N 0
+#define SPKGPU_SQ_8N 1
+#define SPKGPU_SC_6N 2
+#define SPKGPU_SC_26N 3
+
+/* app styles (AppStyle names in src/app_*.h) */
+#define SPKGPU_ISING 0
+#define SPKGPU_POTTS 1
+#define SPKGPU_POTTS_NEIGHONLY 2
+#define SPKGPU_POTTS_NEIGH 3
+
+#define SPKGPU_RNG_PHILOX 0
+#define SPKGPU_RNG_STRICT 1
+
+typedef struct spkgpu_lattice spkgpu_lattice;
+
+typedef struct spkgpu_desc {
+  int32_t lattice;      /* SPKGPU_SQ_4N ... */
+  int32_t nx, ny, nz;   /* sites per axis; nz = 1 for 2d styles */
+  int32_t app;          /* SPKGPU_ISING ... */
+  int32_t nspins;       /* Q (2 for Ising); must be < 2^21 */
+  int32_t spin_bytes;   /* device storage per site: 1, 2, 4, or 0 = smallest
+                           that holds nspins */
+  int32_t nsector;      /* 1 = no sectors, else 2, 4, 8 (`sector`) */
+  int32_t nloop;        /* passes over each set per sweep (`sector nstop`) */
+  int32_t procs[3];     /* processor grid (`processors`), 1 1 1 = serial */
+  int32_t rng;          /* SPKGPU_RNG_PHILOX or SPKGPU_RNG_STRICT */
+  int32_t mask;         /* 1 = `sweep ... mask yes` */
+  uint32_t seed;        /* Philox key word */
+  int32_t device;       /* CUDA device ordinal */
+} spkgpu_desc;
+
+typedef struct spkgpu_stats {
+  int64_t naccept;      /* site values changed (src/app_ising.cpp:124) */
+  int64_t nattempt;     /* site updates attempted */
+  int64_t nsweeps;      /* sweeps done on this handle */
+} spkgpu_stats;
+
+/* lifecycle ------------------------------------------------------------ */
+int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out);
+int spkgpu_destroy(spkgpu_lattice *h);
+const char *spkgpu_last_error(const spkgpu_lattice *h);
+int spkgpu_version(void);
+
+/* `temperature T` (AppLattice::set_temperature, src/app_lattice.cpp:893-898) */
+int spkgpu_set_temperature(spkgpu_lattice *h, double temperature);
+
+/* site values in App::iarray[0] order (site index = id - 1) */
+int spkgpu_upload_spins(spkgpu_lattice *h, const int32_t *spin, int64_t n);
+int spkgpu_download_spins(spkgpu_lattice *h, int32_t *spin, int64_t n);
+/* per-site Park-Miller states for SPKGPU_RNG_STRICT (AppLattice::siteseeds) */
+int spkgpu_upload_siteseeds(spkgpu_lattice *h, const int32_t *seeds, int64_t n);
+int spkgpu_download_siteseeds(spkgpu_lattice *h, int32_t *seeds, int64_t n);
+/* mask bytes for `sweep ... mask yes` (AppLattice::mask) */
+int spkgpu_upload_mask(spkgpu_lattice *h, const uint8_t *mask, int64_t n);
+int spkgpu_download_mask(spkgpu_lattice *h, uint8_t *mask, int64_t n);
+
+/* rejection sweeps --------------------------------------------------------
+   Enqueues nsweeps sweeps on the handle's stream and returns; the sweep
+   index (Philox counter word) continues from the previous call. */
+int spkgpu_sweep(spkgpu_lattice *h, int32_t nsweeps);
+int spkgpu_set_sweep_index(spkgpu_lattice *h, int64_t sweep);
+/* waits for the stream, then reports the counters */
+int spkgpu_get_stats(spkgpu_lattice *h, spkgpu_stats *out);
+/* total energy = sum of site energies (waits for the stream) */
+int spkgpu_energy(spkgpu_lattice *h, double *energy);
+int spkgpu_synchronize(spkgpu_lattice *h);
+/* enqueue nsweeps sweeps bracketed by CUDA events on the handle's stream,
+   wait, and report the elapsed device time in milliseconds */
+int spkgpu_timed_sweeps(spkgpu_lattice *h, int32_t nsweeps, float *ms);
+/* the handle's stream (cudaStream_t) and device spin buffer, for callers
+   that keep their own data resident on the device */
+int spkgpu_stream(spkgpu_lattice *h, void **stream);
+int spkgpu_device_spins(spkgpu_lattice *h, void **dptr, int64_t *bytes);
+/* number of kernel launches this handle has issued */
+int spkgpu_launch_count(const spkgpu_lattice *h, int64_t *count);
+
+/* rejection-free KMC with the tree solver over sectors --------------------
+   adapt = 1: `sector ... nstop N` (dt_kmc = N / max per-site propensity),
+   adapt = 0: `sector ... tstop dt`.  fp64 = 1 computes propensities in FP64
+   (bit-exact mode), 0 in FP32; tree sums and the clock are FP64 always.
+   spkgpu_kmc_run performs one `run` from *time to stoptime. */
+typedef struct spkgpu_kmc_stats {
+  double time;          /* simulated time reached */
+  int64_t naccept;      /* events executed (cumulative) */
+  int64_t npass;        /* passes over all sectors (cumulative) */
+  double dt_kmc;        /* current sector time increment */
+  double total_propensity; /* sum of all tree roots after the run */
+} spkgpu_kmc_stats;
+int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, double tstop, int32_t fp64);
+int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -219,3 +219,27 @@ class Kmc:
         if getattr(self, "h", None):
             lib().spko_kmc_destroy(self.h)
             self.h = None
+
+
+def ranmars_draws(seed: int, n: int) -> list[float]:
+    """The first n RanMars::uniform() values after `seed` (src/random_mars.cpp)."""
+    r = RanMars()
+    lib().spko_ranmars_init(ctypes.byref(r), seed)
+    return [lib().spko_ranmars_uniform(ctypes.byref(r)) for _ in range(n)]
+
+
+def park_seed(rseed: float) -> int:
+    """RandomPark(double) seed (src/random_park.cpp:44-48)."""
+    return lib().spko_park_seed_from_double(rseed)
+
+
+def set_range(park: int, n: int, lo: int, hi: int) -> np.ndarray:
+    """`set site range lo hi` values from a Park-Miller seed (src/set.cpp:598-624)."""
+    s = np.empty(n, dtype=np.int32)
+    lib().spko_set_range(park, n, lo, hi, _ptr(s, ctypes.c_int32))
+    return s
+
+
+def strict_siteseeds(rseed: float, n: int) -> np.ndarray:
+    """Per-site seeds of sweep color/strict: tagreset(rseed, id, 100) (src/app_lattice.cpp:287-295)."""
+    return np.array([lib().spko_park_reset(rseed, i + 1, 100) for i in range(n)], dtype=np.int32)

@@ -1,0 +1,237 @@
+"""spparks_gb300: GB300-native (sm_103a) on-lattice Monte Carlo hot path of SPPARKS.
+
+Python binding (ctypes) over the C ABI in ``include/spkgpu.h``.  Two levels:
+
+* :class:`Lattice` - one lattice on the GPU: the calls a host ``AppLattice``
+  subclass makes (upload site values, set the temperature, sweep, KMC run,
+  download, energy).
+* :class:`SPPARKS` - the reference's library interface (``spparks_open_no_mpi``,
+  ``spparks_command``, ``spparks_file``, ``spparks_extract``, ``spparks_energy``,
+  ``spparks_close``; src/library.h, python/spparks.py) over the repo's own
+  input-script driver, so a script written for the reference's ``sweep color``
+  or ``solve_style tree`` path runs unchanged on the GPU.
+
+There is no CPU fallback: if ``_lib/libspkgpu.so`` is missing or no GPU is
+present the calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_lib" / "libspkgpu.so"
+
+SQ_4N, SQ_8N, SC_6N, SC_26N = 0, 1, 2, 3
+ISING, POTTS, POTTS_NEIGHONLY, POTTS_NEIGH = 0, 1, 2, 3
+RNG_PHILOX, RNG_STRICT = 0, 1
+LATTICE_STYLES = {"sq/4n": SQ_4N, "sq/8n": SQ_8N, "sc/6n": SC_6N, "sc/26n": SC_26N}
+APP_STYLES = {"ising": ISING, "potts": POTTS, "potts/neighonly": POTTS_NEIGHONLY, "potts/neigh": POTTS_NEIGH}
+
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "invalid state", -4: "out of device memory",
+          -5: "unsupported", -6: "invalid site value"}
+
+
+class SpkGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"spkgpu error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [
+        ("lattice", ctypes.c_int32),
+        ("nx", ctypes.c_int32),
+        ("ny", ctypes.c_int32),
+        ("nz", ctypes.c_int32),
+        ("app", ctypes.c_int32),
+        ("nspins", ctypes.c_int32),
+        ("spin_bytes", ctypes.c_int32),
+        ("nsector", ctypes.c_int32),
+        ("nloop", ctypes.c_int32),
+        ("procs", ctypes.c_int32 * 3),
+        ("rng", ctypes.c_int32),
+        ("mask", ctypes.c_int32),
+        ("seed", ctypes.c_uint32),
+        ("device", ctypes.c_int32),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("naccept", ctypes.c_int64), ("nattempt", ctypes.c_int64), ("nsweeps", ctypes.c_int64)]
+
+
+class KmcStats(ctypes.Structure):
+    _fields_ = [("time", ctypes.c_double), ("naccept", ctypes.c_int64), ("npass", ctypes.c_int64),
+                ("dt_kmc", ctypes.c_double), ("total_propensity", ctypes.c_double)]
+
+
+# every symbol include/spkgpu.h (and the other include/*.h) declares
+EXPORTS = [
+    "spkgpu_create", "spkgpu_destroy", "spkgpu_last_error", "spkgpu_version", "spkgpu_set_temperature",
+    "spkgpu_upload_spins", "spkgpu_download_spins", "spkgpu_upload_siteseeds", "spkgpu_download_siteseeds",
+    "spkgpu_upload_mask", "spkgpu_download_mask", "spkgpu_sweep", "spkgpu_set_sweep_index",
+    "spkgpu_get_stats", "spkgpu_energy", "spkgpu_synchronize", "spkgpu_timed_sweeps", "spkgpu_stream",
+    "spkgpu_device_spins", "spkgpu_launch_count", "spkgpu_kmc_setup", "spkgpu_kmc_run",
+]
+
+_lib = None
+
+
+def load_library(path: Path | None = None):
+    """Load libspkgpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise SpkGpuError(-3, f"{p} is missing: build it with `python -m spparks_gb300.build`")
+    L = ctypes.CDLL(str(p))
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    L.spkgpu_create.argtypes = [P(Desc), P(vp)]
+    L.spkgpu_destroy.argtypes = [vp]
+    L.spkgpu_last_error.argtypes = [vp]
+    L.spkgpu_last_error.restype = ctypes.c_char_p
+    L.spkgpu_set_temperature.argtypes = [vp, ctypes.c_double]
+    for name in ("spkgpu_upload_spins", "spkgpu_download_spins", "spkgpu_upload_siteseeds",
+                 "spkgpu_download_siteseeds"):
+        getattr(L, name).argtypes = [vp, P(ctypes.c_int32), ctypes.c_int64]
+    for name in ("spkgpu_upload_mask", "spkgpu_download_mask"):
+        getattr(L, name).argtypes = [vp, P(ctypes.c_uint8), ctypes.c_int64]
+    L.spkgpu_sweep.argtypes = [vp, ctypes.c_int32]
+    L.spkgpu_set_sweep_index.argtypes = [vp, ctypes.c_int64]
+    L.spkgpu_get_stats.argtypes = [vp, P(Stats)]
+    L.spkgpu_energy.argtypes = [vp, P(ctypes.c_double)]
+    L.spkgpu_synchronize.argtypes = [vp]
+    L.spkgpu_timed_sweeps.argtypes = [vp, ctypes.c_int32, P(ctypes.c_float)]
+    L.spkgpu_stream.argtypes = [vp, P(vp)]
+    L.spkgpu_device_spins.argtypes = [vp, P(vp), P(ctypes.c_int64)]
+    L.spkgpu_launch_count.argtypes = [vp, P(ctypes.c_int64)]
+    L.spkgpu_kmc_setup.argtypes = [vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32]
+    L.spkgpu_kmc_run.argtypes = [vp, P(ctypes.c_double), ctypes.c_double, P(KmcStats)]
+    if path is None:
+        _lib = L
+    return L
+
+
+def _i32p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class Lattice:
+    """One lattice on the GPU behind the C ABI."""
+
+    def __init__(self, lattice="sq/4n", nx=16, ny=16, nz=1, app="ising", nspins=2, spin_bytes=0, nsector=1,
+                 nloop=1, procs=(1, 1, 1), rng=RNG_PHILOX, mask=False, seed=12345, device=0):
+        self.lib = load_library()
+        d = Desc()
+        d.lattice = LATTICE_STYLES[lattice] if isinstance(lattice, str) else int(lattice)
+        d.nx, d.ny, d.nz = nx, ny, nz
+        d.app = APP_STYLES[app] if isinstance(app, str) else int(app)
+        d.nspins = nspins
+        d.spin_bytes = spin_bytes
+        d.nsector = nsector
+        d.nloop = nloop
+        d.procs[0], d.procs[1], d.procs[2] = procs
+        d.rng = rng
+        d.mask = int(bool(mask))
+        d.seed = seed & 0xFFFFFFFF
+        d.device = device
+        self.desc = d
+        self.n = nx * ny * nz
+        self.h = ctypes.c_void_p()
+        rc = self.lib.spkgpu_create(ctypes.byref(d), ctypes.byref(self.h))
+        if rc != 0:
+            self.h = None
+            raise SpkGpuError(rc, "spkgpu_create rejected the lattice description")
+
+    def _check(self, rc):
+        if rc != 0:
+            raise SpkGpuError(rc, self.lib.spkgpu_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.spkgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_temperature(self, t: float):
+        self._check(self.lib.spkgpu_set_temperature(self.h, float(t)))
+
+    def upload(self, spin: np.ndarray):
+        s = np.ascontiguousarray(spin, dtype=np.int32)
+        self._check(self.lib.spkgpu_upload_spins(self.h, _i32p(s), s.size))
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.int32) if out is None else out
+        self._check(self.lib.spkgpu_download_spins(self.h, _i32p(out), out.size))
+        return out
+
+    def upload_siteseeds(self, seeds: np.ndarray):
+        s = np.ascontiguousarray(seeds, dtype=np.int32)
+        self._check(self.lib.spkgpu_upload_siteseeds(self.h, _i32p(s), s.size))
+
+    def download_siteseeds(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.int32)
+        self._check(self.lib.spkgpu_download_siteseeds(self.h, _i32p(out), out.size))
+        return out
+
+    def upload_mask(self, mask: np.ndarray):
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        self._check(self.lib.spkgpu_upload_mask(self.h, m.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), m.size))
+
+    def download_mask(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.uint8)
+        self._check(self.lib.spkgpu_download_mask(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                                  out.size))
+        return out
+
+    def sweep(self, nsweeps: int = 1):
+        self._check(self.lib.spkgpu_sweep(self.h, int(nsweeps)))
+
+    def set_sweep_index(self, sweep: int):
+        self._check(self.lib.spkgpu_set_sweep_index(self.h, int(sweep)))
+
+    def timed_sweeps(self, nsweeps: int) -> float:
+        ms = ctypes.c_float()
+        self._check(self.lib.spkgpu_timed_sweeps(self.h, int(nsweeps), ctypes.byref(ms)))
+        return ms.value
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.spkgpu_get_stats(self.h, ctypes.byref(s)))
+        return {"naccept": s.naccept, "nattempt": s.nattempt, "nsweeps": s.nsweeps}
+
+    def energy(self) -> float:
+        e = ctypes.c_double()
+        self._check(self.lib.spkgpu_energy(self.h, ctypes.byref(e)))
+        return e.value
+
+    def synchronize(self):
+        self._check(self.lib.spkgpu_synchronize(self.h))
+
+    def launch_count(self) -> int:
+        c = ctypes.c_int64()
+        self._check(self.lib.spkgpu_launch_count(self.h, ctypes.byref(c)))
+        return c.value
+
+    def kmc_setup(self, adapt=True, nstop=1.0, tstop=0.0, fp64=True):
+        self._check(self.lib.spkgpu_kmc_setup(self.h, int(bool(adapt)), float(nstop), float(tstop),
+                                              int(bool(fp64))))
+
+    def kmc_run(self, time: float, stoptime: float) -> dict:
+        t = ctypes.c_double(time)
+        s = KmcStats()
+        self._check(self.lib.spkgpu_kmc_run(self.h, ctypes.byref(t), float(stoptime), ctypes.byref(s)))
+        return {"time": s.time, "naccept": s.naccept, "npass": s.npass, "dt_kmc": s.dt_kmc,
+                "total_propensity": s.total_propensity}

@@ -1,0 +1,292 @@
+// Generic colour-phase sweep kernel: one launch updates every site of one
+// colour inside one set (a sector of every processor sub-domain, or the whole
+// lattice), the inner loop of AppLattice::iterate_rejection
+// (src/app_lattice.cpp:672-690) with sweep_nomask_nostrict /
+// sweep_mask_nostrict / sweep_nomask_strict / sweep_mask_strict
+// (src/app_lattice.cpp:776-819).  Sites of one colour never neighbour each
+// other (Lattice::ncolors, src/lattice.cpp:187-228), so all of them update
+// in parallel with the same result as the reference's ascending loop.
+//
+// It covers every lattice, app, storage width, sector layout, processor grid,
+// mask and RNG mode; the fused kernels in sweep_fused2d.cu take the common
+// no-sector cases faster.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "site_update.cuh"
+#include "spk_internal.h"
+
+namespace spk {
+
+template <int LAT>
+__device__ __forceinline__ int64_t wrap_index(int x, int y, int z, int dx, int dy, int dz, int nx, int ny,
+                                              int nz) {
+  int xn = x + dx, yn = y + dy, zn = z + dz;
+  xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
+  yn = yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn);
+  if (Stencil<LAT>::k3d) zn = zn < 0 ? zn + nz : (zn >= nz ? zn - nz : zn);
+  else zn = 0;
+  return (int64_t)xn + (int64_t)nx * ((int64_t)yn + (int64_t)ny * zn);
+}
+
+template <typename S, int LAT, int APP>
+__global__ void __launch_bounds__(256) phase_kernel(PhaseArgs a) {
+  constexpr int NN = Stencil<LAT>::NN;
+  __shared__ uint64_t thr[kMaxNeigh + 1];
+  __shared__ double pexp[kMaxNeigh + 1];
+  if (threadIdx.x <= kMaxNeigh) {
+    thr[threadIdx.x] = a.acc.thr[threadIdx.x];
+    pexp[threadIdx.x] = a.acc.pexp[threadIdx.x];
+  }
+  __syncthreads();
+  S *spin = (S *)a.spin;
+  int nxh = a.nxl[0] > a.nxl[1] ? a.nxl[0] : a.nxl[1];
+  int64_t total = (int64_t)nxh * a.nyl * a.nzl;
+  unsigned int changed_count = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int ix = (int)(t % nxh);
+    int64_t r = t / nxh;
+    int iy = (int)(r % a.nyl);
+    int iz = (int)(r / a.nyl);
+    int y = a.yl[iy];
+    int z = a.zl[iz];
+    int q = a.xpar_fixed ? 0 : ((a.color - 1 + y + z) & 1);
+    if (ix >= a.nxl[q]) continue;
+    int x = a.xl[q][ix];
+    int64_t i = (int64_t)x + (int64_t)a.nx * ((int64_t)y + (int64_t)a.ny * z);
+    if (a.mask_on && a.mask[i]) continue;
+    int own = (int)spin[i];
+    int nb[NN];
+#pragma unroll
+    for (int j = 0; j < NN; j++) {
+      int dx, dy, dz;
+      Stencil<LAT>::offset(j, dx, dy, dz);
+      nb[j] = (int)spin[wrap_index<LAT>(x, y, z, dx, dy, dz, a.nx, a.ny, a.nz)];
+    }
+    int news, e0;
+    if (a.rng == SPKGPU_RNG_PHILOX) {
+      U4 w = sweep_block(a.seed, (uint64_t)i, a.sweep, a.pass);
+      uint32_t x0 = (i & 1) ? w.z : w.x;
+      uint32_t x1 = (i & 1) ? w.w : w.y;
+      news = update_philox<NN, APP>(own, nb, x0, x1, a.nspins, thr, a.acc.zero_t, &e0);
+    } else {
+      int pm = a.siteseeds[i];
+      news = update_strict<NN, APP>(own, nb, pm, a.nspins, pexp, a.acc.zero_t, &e0);
+      a.siteseeds[i] = pm;
+    }
+    if (news != own) {
+      spin[i] = (S)news;
+      changed_count++;
+    }
+    if (a.mask_on) {
+      // AppIsing::site_event_rejection mask update (src/app_ising.cpp:131-135)
+      if (2 * e0 < NN) a.mask[i] = 1;
+      if (news != own) {
+#pragma unroll
+        for (int j = 0; j < NN; j++) {
+          int dx, dy, dz;
+          Stencil<LAT>::offset(j, dx, dy, dz);
+          a.mask[wrap_index<LAT>(x, y, z, dx, dy, dz, a.nx, a.ny, a.nz)] = 0;
+        }
+      }
+    }
+  }
+  unsigned int warp_sum = __reduce_add_sync(0xFFFFFFFFu, changed_count);
+  if ((threadIdx.x & 31) == 0 && warp_sum) atomicAdd(a.naccept, (unsigned long long)warp_sum);
+}
+
+template <typename S, int LAT>
+static cudaError_t launch_phase_app(int app, const PhaseArgs &a, cudaStream_t s, int num_sms) {
+  int nxh = a.nxl[0] > a.nxl[1] ? a.nxl[0] : a.nxl[1];
+  int64_t total = (int64_t)nxh * a.nyl * a.nzl;
+  if (total <= 0) return cudaSuccess;
+  int64_t blocks = (total + 255) / 256;
+  int64_t cap = (int64_t)num_sms * 8;
+  if (blocks > cap) blocks = cap;
+  dim3 grid((unsigned)blocks);
+  switch (app) {
+    case SPKGPU_ISING: phase_kernel<S, LAT, SPKGPU_ISING><<<grid, 256, 0, s>>>(a); break;
+    case SPKGPU_POTTS: phase_kernel<S, LAT, SPKGPU_POTTS><<<grid, 256, 0, s>>>(a); break;
+    case SPKGPU_POTTS_NEIGHONLY: phase_kernel<S, LAT, SPKGPU_POTTS_NEIGHONLY><<<grid, 256, 0, s>>>(a); break;
+    case SPKGPU_POTTS_NEIGH: phase_kernel<S, LAT, SPKGPU_POTTS_NEIGH><<<grid, 256, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <typename S>
+static cudaError_t launch_phase_lat(int lattice, int app, const PhaseArgs &a, cudaStream_t s, int num_sms) {
+  switch (lattice) {
+    case SPKGPU_SQ_4N: return launch_phase_app<S, SPKGPU_SQ_4N>(app, a, s, num_sms);
+    case SPKGPU_SQ_8N: return launch_phase_app<S, SPKGPU_SQ_8N>(app, a, s, num_sms);
+    case SPKGPU_SC_6N: return launch_phase_app<S, SPKGPU_SC_6N>(app, a, s, num_sms);
+    case SPKGPU_SC_26N: return launch_phase_app<S, SPKGPU_SC_26N>(app, a, s, num_sms);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_phase(int lattice, int app, int spin_bytes, const PhaseArgs &a, cudaStream_t s,
+                         int num_sms) {
+  switch (spin_bytes) {
+    case 1: return launch_phase_lat<int8_t>(lattice, app, a, s, num_sms);
+    case 2: return launch_phase_lat<int16_t>(lattice, app, a, s, num_sms);
+    case 4: return launch_phase_lat<int32_t>(lattice, app, a, s, num_sms);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// mask clearing before a set is swept
+
+template <int LAT>
+__global__ void mask_clear_kernel(MaskClearArgs a) {
+  constexpr int NN = Stencil<LAT>::NN;
+  int64_t total = (int64_t)a.nxl * a.nyl * a.nzl;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int x = a.xl[t % a.nxl];
+    int64_t r = t / a.nxl;
+    int y = a.yl[r % a.nyl];
+    int z = a.zl[r / a.nyl];
+    int64_t i = (int64_t)x + (int64_t)a.nx * ((int64_t)y + (int64_t)a.ny * z);
+    if (a.color > 0) {
+      if (Stencil<LAT>::color(x, y, z) == a.color) a.mask[i] = 0;
+      continue;
+    }
+    int px = a.proc_x[x], py = a.proc_y[y], pz = a.proc_z[z];
+    int hx = a.half_x[x], hy = a.half_y[y], hz = a.half_z[z];
+    bool border = false;
+#pragma unroll
+    for (int j = 0; j < NN; j++) {
+      int dx, dy, dz;
+      Stencil<LAT>::offset(j, dx, dy, dz);
+      int xn = x + dx, yn = y + dy, zn = z + dz;
+      xn = xn < 0 ? xn + a.nx : (xn >= a.nx ? xn - a.nx : xn);
+      yn = yn < 0 ? yn + a.ny : (yn >= a.ny ? yn - a.ny : yn);
+      zn = Stencil<LAT>::k3d ? (zn < 0 ? zn + a.nz : (zn >= a.nz ? zn - a.nz : zn)) : 0;
+      if (a.proc_x[xn] != px || a.proc_y[yn] != py || a.proc_z[zn] != pz || a.half_x[xn] != hx ||
+          a.half_y[yn] != hy || a.half_z[zn] != hz)
+        border = true;
+    }
+    if (border) a.mask[i] = 0;
+  }
+}
+
+cudaError_t launch_mask_clear(int lattice, const MaskClearArgs &a, cudaStream_t s, int num_sms) {
+  int64_t total = (int64_t)a.nxl * a.nyl * a.nzl;
+  if (total <= 0) return cudaSuccess;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+  switch (lattice) {
+    case SPKGPU_SQ_4N: mask_clear_kernel<SPKGPU_SQ_4N><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case SPKGPU_SQ_8N: mask_clear_kernel<SPKGPU_SQ_8N><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case SPKGPU_SC_6N: mask_clear_kernel<SPKGPU_SC_6N><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case SPKGPU_SC_26N: mask_clear_kernel<SPKGPU_SC_26N><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// total energy: sum over sites of the unlike-neighbour count
+// (spparks_energy, src/library.cpp:140-146)
+
+template <typename S, int LAT>
+__global__ void energy_kernel(const S *spin, int nx, int ny, int nz, unsigned long long *out) {
+  constexpr int NN = Stencil<LAT>::NN;
+  int64_t n = (int64_t)nx * ny * nz;
+  unsigned long long e = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int x = (int)(i % nx);
+    int64_t r = i / nx;
+    int y = (int)(r % ny);
+    int z = (int)(r / ny);
+    int own = spin[i];
+#pragma unroll
+    for (int j = 0; j < NN; j++) {
+      int dx, dy, dz;
+      Stencil<LAT>::offset(j, dx, dy, dz);
+      e += (spin[wrap_index<LAT>(x, y, z, dx, dy, dz, nx, ny, nz)] != own);
+    }
+  }
+  unsigned long long w = e;
+  for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xFFFFFFFFu, w, o);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(out, w);
+}
+
+template <typename S>
+static cudaError_t launch_energy_t(int lattice, const void *spin, int nx, int ny, int nz, unsigned long long *out,
+                                   cudaStream_t s, int num_sms) {
+  int64_t n = (int64_t)nx * ny * nz;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+  const S *p = (const S *)spin;
+  switch (lattice) {
+    case SPKGPU_SQ_4N: energy_kernel<S, SPKGPU_SQ_4N><<<(unsigned)blocks, 256, 0, s>>>(p, nx, ny, nz, out); break;
+    case SPKGPU_SQ_8N: energy_kernel<S, SPKGPU_SQ_8N><<<(unsigned)blocks, 256, 0, s>>>(p, nx, ny, nz, out); break;
+    case SPKGPU_SC_6N: energy_kernel<S, SPKGPU_SC_6N><<<(unsigned)blocks, 256, 0, s>>>(p, nx, ny, nz, out); break;
+    case SPKGPU_SC_26N: energy_kernel<S, SPKGPU_SC_26N><<<(unsigned)blocks, 256, 0, s>>>(p, nx, ny, nz, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_energy(int lattice, int spin_bytes, const void *spin, int nx, int ny, int nz,
+                          unsigned long long *out, cudaStream_t s, int num_sms) {
+  switch (spin_bytes) {
+    case 1: return launch_energy_t<int8_t>(lattice, spin, nx, ny, nz, out, s, num_sms);
+    case 2: return launch_energy_t<int16_t>(lattice, spin, nx, ny, nz, out, s, num_sms);
+    case 4: return launch_energy_t<int32_t>(lattice, spin, nx, ny, nz, out, s, num_sms);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// int32 <-> storage width, with the value check of AppIsing/AppPotts::init_app
+// (src/app_ising.cpp:63-70, src/app_potts.cpp:78-84)
+
+template <typename S>
+__global__ void convert_in_kernel(const int32_t *src, S *dst, int64_t n, int nspins, int *bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int v = src[i];
+    if (v < 1 || v > nspins) *bad = 1;
+    dst[i] = (S)v;
+  }
+}
+
+template <typename S>
+__global__ void convert_out_kernel(const S *src, int32_t *dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (int32_t)src[i];
+}
+
+cudaError_t launch_convert_in(int spin_bytes, const int32_t *src, void *dst, int64_t n, int nspins, int *bad,
+                              cudaStream_t s) {
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  if (n <= 0) return cudaSuccess;
+  switch (spin_bytes) {
+    case 1: convert_in_kernel<int8_t><<<(unsigned)blocks, 256, 0, s>>>(src, (int8_t *)dst, n, nspins, bad); break;
+    case 2: convert_in_kernel<int16_t><<<(unsigned)blocks, 256, 0, s>>>(src, (int16_t *)dst, n, nspins, bad); break;
+    case 4: convert_in_kernel<int32_t><<<(unsigned)blocks, 256, 0, s>>>(src, (int32_t *)dst, n, nspins, bad); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_convert_out(int spin_bytes, const void *src, int32_t *dst, int64_t n, cudaStream_t s) {
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  if (n <= 0) return cudaSuccess;
+  switch (spin_bytes) {
+    case 1: convert_out_kernel<int8_t><<<(unsigned)blocks, 256, 0, s>>>((const int8_t *)src, dst, n); break;
+    case 2: convert_out_kernel<int16_t><<<(unsigned)blocks, 256, 0, s>>>((const int16_t *)src, dst, n); break;
+    case 4: convert_out_kernel<int32_t><<<(unsigned)blocks, 256, 0, s>>>((const int32_t *)src, dst, n); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace spk

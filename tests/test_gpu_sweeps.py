@@ -1,0 +1,145 @@
+"""GPU parity of the colour-sweep path (spkgpu_sweep through the C ABI).
+
+Lattices must be bit-identical to the reference (fixtures produced by the
+reference built with the Philox RandomPark shim, and by the unmodified
+reference for sweep color/strict) and to the oracle restatement after every
+sweep; Naccept/Nattempt must match exactly."""
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sg():
+    import spparks_gb300
+
+    spparks_gb300.load_library()
+    return spparks_gb300
+
+
+def make_lattice(sg, case, spin_bytes=0, rng=0, seed=None, procs=(1, 1, 1)):
+    return sg.Lattice(case["lattice"], case["nx"], case["ny"], case["nz"], case["app"], case["nspins"],
+                      spin_bytes=spin_bytes, nsector=case.get("nsector", 1), nloop=case.get("nloop", 1),
+                      procs=procs, rng=rng, mask=case.get("mask", False),
+                      seed=case.get("seed", 0) if seed is None else seed)
+
+
+@pytest.mark.parametrize("k", range(13))
+def test_sweeps_match_reference_fixtures(sg, ref_fixtures, k):
+    fx = ref_fixtures["sweeps"][k]
+    case = fx["case"]
+    init = np.array(fx["snaps"]["init"]["spins"], dtype=np.int32)
+    for sb in (1, 2, 4):
+        if sb == 1 and case["nspins"] > 127:
+            continue
+        lat = make_lattice(sg, case, spin_bytes=sb)
+        lat.set_temperature(case["temperature"])
+        lat.upload(init)
+        hashes = []
+        for s in range(case["nsweeps"]):
+            lat.sweep(1)
+            hashes.append(format(oracle.spin_hash(lat.download()), "016x"))
+        assert hashes == [r[3] for r in fx["sweeps"]], (case["name"], sb)
+        st = lat.stats()
+        assert (st["naccept"], st["nattempt"]) == (fx["sweeps"][-1][1], fx["sweeps"][-1][2])
+        assert lat.download().tolist() == fx["snaps"]["final"]["spins"]
+        lat.close()
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_strict_matches_unmodified_reference(sg, ref_fixtures, k):
+    fx = ref_fixtures["strict"][k]
+    case = fx["case"]
+    n = case["nx"] * case["ny"] * case["nz"]
+    u = oracle.ranmars_draws(case["master_seed"], 5)
+    spin = oracle.set_range(oracle.park_seed(u[0]), n, 1, case["nspins"])
+    seeds = oracle.strict_siteseeds(u[4], n)
+    lat = make_lattice(sg, case, rng=1, seed=0)
+    lat.set_temperature(case["temperature"])
+    lat.upload(spin)
+    lat.upload_siteseeds(seeds)
+    for r in range(case["nruns"]):
+        lat.sweep(case["sweeps_per_run"])
+        assert lat.download().tolist() == fx["snaps"][f"run{r}"]["spins"]
+        assert lat.energy() == fx["energies"][r]
+    lat.close()
+
+
+RANDOM_CASES = [
+    dict(lattice="sq/4n", nx=64, ny=48, nz=1, app="potts", nspins=50, temperature=0.9),
+    dict(lattice="sq/8n", nx=40, ny=40, nz=1, app="potts/neighonly", nspins=30, temperature=0.4),
+    dict(lattice="sc/6n", nx=16, ny=12, nz=10, app="ising", nspins=2, temperature=4.5115),
+    dict(lattice="sc/26n", nx=12, ny=12, nz=12, app="potts/neighonly", nspins=100, temperature=0.5),
+    dict(lattice="sc/26n", nx=10, ny=8, nz=6, app="potts/neigh", nspins=7, temperature=1.3),
+    dict(lattice="sq/4n", nx=32, ny=32, nz=1, app="ising", nspins=2, temperature=1.1345, nsector=4),
+    dict(lattice="sc/6n", nx=12, ny=12, nz=12, app="potts", nspins=5, temperature=0.7, nsector=8),
+]
+
+
+@pytest.mark.parametrize("case", RANDOM_CASES, ids=lambda c: f"{c['app']}-{c['lattice']}-{c.get('nsector', 1)}")
+def test_random_cases_match_oracle(sg, case):
+    seed = 97531
+    n = case["nx"] * case["ny"] * case["nz"]
+    spin = oracle.init_spins(seed, n, 1, case["nspins"])
+    cfg = oracle.make_cfg(case["lattice"], case["nx"], case["ny"], case["nz"], case["app"], case["nspins"],
+                          case["temperature"], case.get("nsector", 1), 1, 0, seed)
+    ref = spin.copy()
+    na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 5)
+    lat = make_lattice(sg, case, seed=seed)
+    lat.set_temperature(case["temperature"])
+    lat.upload(spin)
+    got = []
+    for s in range(5):
+        lat.sweep(1)
+        got.append(oracle.spin_hash(lat.download()))
+    assert got == [int(h) for h in hashes]
+    st = lat.stats()
+    assert (st["naccept"], st["nattempt"]) == (na, nt)
+
+
+@pytest.mark.parametrize("procs,nsector", [((2, 2, 1), 4), ((3, 1, 1), 2), ((2, 1, 1), 1)])
+def test_processor_grid_sectors_match_oracle(sg, procs, nsector):
+    """`processors Px Py 1` + `sector`: sector k of every sub-domain is one set
+    (the reference's parallel ordering, src/app_lattice.cpp:648-699)."""
+    case = dict(lattice="sq/8n", nx=24, ny=20, nz=1, app="potts", nspins=9, temperature=0.8, nsector=nsector)
+    seed = 4242
+    n = 24 * 20
+    spin = oracle.init_spins(seed, n, 1, 9)
+    cfg = oracle.make_cfg("sq/8n", 24, 20, 1, "potts", 9, 0.8, nsector, 1, 0, seed, procs=procs)
+    ref = spin.copy()
+    na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 4)
+    lat = make_lattice(sg, case, seed=seed, procs=procs)
+    lat.set_temperature(0.8)
+    lat.upload(spin)
+    lat.sweep(4)
+    assert lat.download().tolist() == ref.tolist()
+    assert lat.stats()["naccept"] == na
+
+
+def test_invalid_spin_rejected(sg):
+    lat = sg.Lattice("sq/4n", 8, 8, 1, "potts", 5)
+    bad = np.full(64, 3, dtype=np.int32)
+    bad[17] = 6
+    with pytest.raises(sg.SpkGpuError) as ei:
+        lat.upload(bad)
+    assert ei.value.code == -6
+
+
+def test_sweep_before_temperature_is_an_error(sg):
+    lat = sg.Lattice("sq/4n", 8, 8, 1, "ising", 2)
+    with pytest.raises(sg.SpkGpuError) as ei:
+        lat.sweep(1)
+    assert ei.value.code == -3
+
+
+def test_energy_matches_oracle(sg):
+    seed = 5
+    spin = oracle.init_spins(seed, 20 * 20 * 20, 1, 40)
+    lat = sg.Lattice("sc/26n", 20, 20, 20, "potts", 40, seed=seed)
+    lat.upload(spin)
+    cfg = oracle.make_cfg("sc/26n", 20, 20, 20, "potts", 40)
+    assert lat.energy() == oracle.energy(cfg, spin)

@@ -79,16 +79,6 @@ def test_kmc_matches_reference(ref_fixtures, k):
     assert km.naccept == ref[-1][1]
 
 
-def ranmars_draws(seed, n):
-    r = oracle.RanMars()
-    oracle.lib().spko_ranmars_init(oracle.ctypes.byref(r), seed)
-    return [oracle.lib().spko_ranmars_uniform(oracle.ctypes.byref(r)) for _ in range(n)]
-
-
-def park_seed(d):
-    return oracle.lib().spko_park_seed_from_double(d)
-
-
 @pytest.mark.parametrize("k", range(3))
 def test_strict_matches_unmodified_reference(ref_fixtures, k):
     """sweep color/strict with the reference's own RanMars/Park-Miller seeding:
@@ -98,11 +88,10 @@ def test_strict_matches_unmodified_reference(ref_fixtures, k):
     case = fx["case"]
     cfg = cfg_from_case(case, rng=oracle.RNG_STRICT, seed=0)
     n = case["nx"] * case["ny"] * case["nz"]
-    u = ranmars_draws(case["master_seed"], 5)
-    spin = np.empty(n, dtype=np.int32)
-    oracle.lib().spko_set_range(park_seed(u[0]), n, 1, case["nspins"], oracle._ptr(spin, oracle.ctypes.c_int32))
+    u = oracle.ranmars_draws(case["master_seed"], 5)
+    spin = oracle.set_range(oracle.park_seed(u[0]), n, 1, case["nspins"])
     assert spin.tolist() == fx["snaps"]["init"]["spins"]
-    seeds = np.array([oracle.lib().spko_park_reset(u[4], i + 1, 100) for i in range(n)], dtype=np.int32)
+    seeds = oracle.strict_siteseeds(u[4], n)
     sweep = 0
     for r in range(case["nruns"]):
         oracle.color_sweeps(cfg, spin, sweep, case["sweeps_per_run"], siteseeds=seeds)
@@ -122,12 +111,10 @@ def example_run(example_logs, which, rows):
         cfg = oracle.make_cfg("sc/26n", 20, 20, 20, "potts", 100, 0.0, nsector=8)
         q = 100
     n = oracle.nsites(cfg)
-    u = ranmars_draws(56789, 3)
-    spin = np.empty(n, dtype=np.int32)
-    oracle.lib().spko_set_range(park_seed(u[0]), n, 1, q, oracle._ptr(spin, oracle.ctypes.c_int32))
+    u = oracle.ranmars_draws(56789, 3)
+    spin = oracle.set_range(oracle.park_seed(u[0]), n, 1, q)
+    # ranapp = RandomPark(u[1]) then reset(u[2], me=0, 100): the reset wins
     ranapp = np.array([oracle.lib().spko_park_reset(u[2], 0, 100)], dtype=np.int32)
-    ranapp[0] = oracle.lib().spko_park_reset(u[2], 0, 100)
-    # RandomPark(u[1]) is overwritten by reset(u[2], me=0, 100)
     log = example_logs[which]["rows"]
     assert oracle.energy(cfg, spin) == log[0]["energy"]
     done = 0
