@@ -1,0 +1,367 @@
+"""Benchmark of the GB300 on-lattice Monte Carlo hot path.
+
+Workload (the configuration the headline metric is quoted on): the batched
+2D Ising ensemble - 512 independent sq/4n replicas with L drawn log-uniform in
+[64, 1024] and rounded to a multiple of 32, kT uniform in [1.5, 3.5], int8
+spins uniform from the seed, replica exchange between neighbouring
+temperatures (of equal-L replicas) every 10 sweeps, 2000 sweeps in all.
+One step = 10 sweeps of every replica plus one exchange round = one replay of
+a captured CUDA graph holding one persistent cooperative launch.
+
+  value      site-updates/s with the spins resident in HBM (CUDA events)
+  e2e        the same through the C ABI with pinned host buffers: each step
+             uploads every replica's int32 site values, runs the step and
+             downloads them (the host<->device sync of a host AppLattice)
+  plain_gpu  the same ensemble swept replica by replica with the plain
+             per-colour phase kernel (a bounded sample, extrapolated)
+  roofline   algorithmic HBM bytes (2 bytes per int8 site-update) / kernel
+             time, against the measured copy bandwidth
+  cpu_baseline  the oracle port (C restatement of the reference's colour
+             sweep) on the host cores over a bounded sample
+
+`--impl reference` times that CPU implementation alone on all host cores
+(the reference sources are not present on the GPU host; its compiled x86
+build cannot run there) and prints the same JSON line.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "site-updates/s on 1 GB300, batched vs plain GPU sweep; % of HBM roofline"
+UNIT = "site-updates/s"
+SEED = 56789
+NREP = 512
+SWEEPS_PER_STEP = 10
+FULL_SWEEPS = 2000
+
+
+def ensemble_config(seed=SEED, nrep=NREP):
+    """Replica sizes and temperatures of the batched workload (seeded)."""
+    rng = np.random.default_rng(seed)
+    L = 32 * np.round(np.exp(rng.uniform(math.log(64), math.log(1024), nrep)) / 32).astype(np.int64)
+    L = np.clip(L, 64, 1024).astype(np.int32)
+    T = rng.uniform(1.5, 3.5, nrep)
+    return L, T
+
+
+def init_spins(L, seed=SEED):
+    rng = np.random.default_rng(seed + 1)
+    n = int(np.sum(L.astype(np.int64) ** 2))
+    return (rng.integers(1, 3, n, dtype=np.int32)).astype(np.int32)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name="ensemble_kernel"):
+    """Per-launch DRAM traffic of the ensemble kernel from the committed ncu
+    summary (profiles/*.md, line `traffic_bytes_per_launch: N`)."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        m = re.search(rf"{name}.*?traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text(), re.S)
+        if m:
+            return float(m.group(1)), f.name
+    return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU implementation (oracle port) - reference arm and cpu_baseline
+
+
+def _cpu_worker(args):
+    reps, sweeps, seed = args
+    import oracle
+
+    done = 0
+    t0 = time.perf_counter()
+    for r, L, T in reps:
+        cfg = oracle.make_cfg("sq/4n", L, L, 1, "ising", 2, T, seed=seed, stream_base=(r + 1) << 8)
+        spin = oracle.init_spins(seed + r, L * L, 1, 2)
+        oracle.color_sweeps(cfg, spin, 0, sweeps)
+        done += L * L * sweeps
+    return done, time.perf_counter() - t0
+
+
+def cpu_rate(sample_replicas=24, sweeps=4, procs=1):
+    """Site-updates/s of the oracle's colour sweep on a sample of replicas."""
+    import multiprocessing as mp
+
+    L, T = ensemble_config()
+    rng = np.random.default_rng(7)
+    pick = rng.choice(len(L), size=min(sample_replicas, len(L)), replace=False)
+    reps = [(int(r), int(L[r]), float(T[r])) for r in pick]
+    chunks = [reps[i::procs] for i in range(procs)]
+    t0 = time.perf_counter()
+    if procs == 1:
+        results = [_cpu_worker((chunks[0], sweeps, SEED))]
+    else:
+        with mp.get_context("spawn").Pool(procs) as pool:
+            results = pool.map(_cpu_worker, [(c, sweeps, SEED) for c in chunks])
+    wall = time.perf_counter() - t0
+    updates = sum(r[0] for r in results)
+    return updates / wall, updates, wall
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build()
+    procs = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_rate(sample_replicas=procs, sweeps=1, procs=procs)
+    rates, times, ups = [], [], 0
+    for _ in range(args.steps):
+        r, u, w = cpu_rate(sample_replicas=2 * procs, sweeps=2, procs=procs)
+        rates.append(r)
+        times.append(w)
+        ups += u
+    value = ups / sum(times)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": "batched 2D Ising ensemble, 512 sq/4n replicas L in [64,1024], kT in [1.5,3.5], "
+                               "exchange every 10 sweeps", "step": "2 sweeps of a random sample of replicas",
+                   "threads": procs},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{2 * procs} replicas x 2 sweeps per step, oracle C restatement of "
+                                   "AppIsing::site_event_rejection + colour sweep, one process per core"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+
+def dist_setup(ngpus):
+    if ngpus <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    world = int(os.environ["WORLD_SIZE"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, world, dist
+
+
+def run_ours(args):
+    import torch
+
+    import spparks_gb300 as sg
+
+    rank, world, dist = dist_setup(args.gpus)
+    device = int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0
+    torch.cuda.set_device(device)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    # each rank runs its own ensemble (independent replicas; no collective)
+    L, T = ensemble_config(seed=SEED + rank)
+    spins = init_spins(L, seed=SEED + rank)
+    nsites = int(np.sum(L.astype(np.int64) ** 2))
+    ens = sg.Ensemble(L, T, "ising", 2, seed=SEED + rank, exchange_every=SWEEPS_PER_STEP, device=device)
+    ens.upload(spins)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")  # > 126 MB L2
+
+    for _ in range(args.warmup):
+        ens.run(SWEEPS_PER_STEP)
+    ens.synchronize()
+
+    # device-resident timed region: one graph replay per step, L2 flushed between steps
+    launches0 = ens.launch_count()
+    clocks = ClockSampler(device)
+    clocks.start()
+    barrier()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step_ms.append(ens.timed_run(SWEEPS_PER_STEP))
+    barrier()
+    clk = clocks.stop()
+    launches = ens.launch_count() - launches0
+    st = ens.stats()
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    updates_rank = nsites * SWEEPS_PER_STEP * args.steps
+    value = updates_rank * world / (total_ms * 1e-3)
+    ms_step = total_ms / args.steps
+
+    # end to end through the C ABI with pinned host buffers
+    host_in = torch.from_numpy(spins).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    ein, eout = host_in.numpy(), host_out.numpy()
+    e2e_steps = max(1, min(args.steps, 20))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ens.upload(ein)
+        ens.run(SWEEPS_PER_STEP)
+        ens.download(eout)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = nsites * SWEEPS_PER_STEP * e2e_steps * world / e2e_s
+
+    # plain GPU sweep: the same replicas one by one with the per-colour phase
+    # kernel (a sample of replicas, 10 sweeps each, extrapolated by sites)
+    rng = np.random.default_rng(11)
+    pick = rng.choice(len(L), size=48, replace=False)
+    plain_ms, plain_sites = 0.0, 0
+    for r in pick:
+        lat = sg.Lattice("sq/4n", int(L[r]), int(L[r]), 1, "ising", 2, spin_bytes=1, seed=SEED, variant=1)
+        lat.set_temperature(float(T[r]))
+        lat.upload(ens.replica(spins, r))
+        lat.timed_sweeps(2)
+        plain_ms += lat.timed_sweeps(SWEEPS_PER_STEP)
+        plain_sites += int(L[r]) ** 2 * SWEEPS_PER_STEP
+        lat.close()
+    plain_rate = plain_sites / (plain_ms * 1e-3)
+
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 2.0 * 1.0 * nsites * SWEEPS_PER_STEP  # int8: read + write of each site per update
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    traffic, traffic_src = profile_traffic()
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+
+        oracle.build()
+        r1, u1, w1 = cpu_rate(sample_replicas=6, sweeps=4, procs=1)
+        cpu = {"value": r1, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"6 random replicas x 4 sweeps ({u1:.3g} site-updates, {w1:.1f} s), oracle C "
+                         "restatement of the reference colour sweep, 1 thread"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int8", "data": "synthetic (seeded replicas, uniform spins)",
+        "config": {"workload": "batched 2D Ising ensemble: 512 sq/4n replicas, L log-uniform in [64,1024] "
+                               "rounded to 32, kT uniform [1.5,3.5], exchange every 10 sweeps",
+                   "replicas": int(len(L)), "sites": nsites, "sweeps_per_step": SWEEPS_PER_STEP,
+                   "full_job_sweeps": FULL_SWEEPS, "l2": "flushed between steps (256 MiB memset)",
+                   "parallelism": f"replicas, {world} independent ensemble(s)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(nsites * 4),
+                "d2h_bytes_per_step": int(nsites * 4), "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "plain_gpu": {"value": plain_rate, "unit": UNIT, "sample": "48 replicas x 10 sweeps, per-colour "
+                      "phase kernel, one lattice at a time", "batched_over_plain": value / world / plain_rate},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": f"{peak_kind} copy bandwidth (burst)", "traffic": traffic,
+                     "traffic_source": traffic_src,
+                     "alg_bytes_per_launch": alg_bytes, "kernel": "ensemble_kernel (one launch per step)"},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "exchange": {"tries": st["exchange_tries"], "accepts": st["exchange_accepts"]},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

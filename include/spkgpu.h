@@ -46,6 +46,7 @@ extern "C" {
 #define SPKGPU_ERR_NOMEM (-4)       /* device allocation failed */
 #define SPKGPU_ERR_UNSUPPORTED (-5) /* combination not implemented */
 #define SPKGPU_ERR_INVALID_SPIN (-6) /* a site value is outside 1..nspins */
+#define SPKGPU_ERR_DEVICE (-7)      /* a device-side wait gave up (error flag set) */
 
 /* lattice styles (src/lattice.cpp:43-57); periodic boxes only */
 #define SPKGPU_SQ_4N 0
@@ -78,6 +79,8 @@ typedef struct spkgpu_desc {
   int32_t mask;         /* 1 = `sweep ... mask yes` */
   uint32_t seed;        /* Philox key word */
   int32_t device;       /* CUDA device ordinal */
+  int32_t variant;      /* 0 = fastest kernel for the configuration,
+                           1 = always the per-colour phase kernel */
 } spkgpu_desc;
 
 typedef struct spkgpu_stats {
@@ -139,6 +142,51 @@ typedef struct spkgpu_kmc_stats {
 } spkgpu_kmc_stats;
 int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, double tstop, int32_t fp64);
 int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_stats *out);
+
+/* batched ensemble of independent sq/4n lattices ---------------------------
+   Many replicas of uneven size L x L (L a multiple of 32) and their own
+   temperatures swept together by one persistent cooperative kernel, with
+   parallel-tempering replica exchange between neighbouring temperatures of
+   equal-L replicas every exchange_every sweeps, on the device.  Each replica
+   follows the same per-site rule as a single `sweep color` lattice (same as
+   spkgpu_sweep with sq/4n); replica r draws from Philox stream (r+1) << 8.
+   The reference has no ensemble; it corresponds to running one reference
+   instance per replica (src/app_lattice.cpp:632-711).  Site values of
+   replica r occupy L_r*L_r consecutive int32 entries, replicas in order. */
+typedef struct spkgpu_ensemble spkgpu_ensemble;
+typedef struct spkgpu_ensemble_desc {
+  int32_t nreplica;
+  const int32_t *L;           /* per-replica edge, multiple of 32 */
+  const double *temperature;  /* per-replica initial temperature (> 0) */
+  int32_t app;                /* SPKGPU_ISING or SPKGPU_POTTS (nspins <= 127) */
+  int32_t nspins;
+  uint32_t seed;
+  int32_t exchange_every;     /* sweeps between exchange rounds, 0 = never */
+  int32_t device;
+} spkgpu_ensemble_desc;
+typedef struct spkgpu_ensemble_stats {
+  int64_t naccept;            /* site values changed, all replicas */
+  int64_t nattempt;
+  int64_t nsweeps;
+  int64_t exchange_tries;
+  int64_t exchange_accepts;
+} spkgpu_ensemble_stats;
+int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **out);
+int spkgpu_ensemble_destroy(spkgpu_ensemble *e);
+const char *spkgpu_ensemble_last_error(const spkgpu_ensemble *e);
+int spkgpu_ensemble_upload(spkgpu_ensemble *e, const int32_t *spin, int64_t n);
+int spkgpu_ensemble_download(spkgpu_ensemble *e, int32_t *spin, int64_t n);
+/* enqueue nsweeps sweeps (a multiple of exchange_every when exchanging);
+   runs as replays of a captured CUDA graph of one persistent launch */
+int spkgpu_ensemble_run(spkgpu_ensemble *e, int32_t nsweeps);
+int spkgpu_ensemble_timed_run(spkgpu_ensemble *e, int32_t nsweeps, float *ms);
+int spkgpu_ensemble_synchronize(spkgpu_ensemble *e);
+int spkgpu_ensemble_get_stats(spkgpu_ensemble *e, spkgpu_ensemble_stats *out);
+/* current temperature of each replica and energy (unlike-neighbour bonds,
+   each counted once) measured at the last exchange round */
+int spkgpu_ensemble_temperatures(spkgpu_ensemble *e, double *temperature);
+int spkgpu_ensemble_energies(spkgpu_ensemble *e, int64_t *bonds);
+int spkgpu_ensemble_launch_count(const spkgpu_ensemble *e, int64_t *count);
 
 #ifdef __cplusplus
 }

@@ -64,6 +64,7 @@ class Cfg(ctypes.Structure):
         ("px", ctypes.c_int),
         ("py", ctypes.c_int),
         ("pz", ctypes.c_int),
+        ("stream_base", ctypes.c_uint32),
     ]
 
 
@@ -133,9 +134,9 @@ def _ptr(a, ctype):
 
 
 def make_cfg(lattice="sq/4n", nx=8, ny=8, nz=1, app="ising", nspins=2, temperature=0.0, nsector=1,
-             nloop=1, rng=RNG_PHILOX, seed=1, mask=0, procs=(1, 1, 1)) -> Cfg:
+             nloop=1, rng=RNG_PHILOX, seed=1, mask=0, procs=(1, 1, 1), stream_base=0) -> Cfg:
     return Cfg(LATTICES[lattice], nx, ny, nz, APPS[app], nspins, float(temperature), nsector, nloop, rng,
-               seed & 0xFFFFFFFF, int(mask), procs[0], procs[1], procs[2])
+               seed & 0xFFFFFFFF, int(mask), procs[0], procs[1], procs[2], stream_base)
 
 
 def philox(ctr, key):
@@ -243,3 +244,71 @@ def set_range(park: int, n: int, lo: int, hi: int) -> np.ndarray:
 def strict_siteseeds(rseed: float, n: int) -> np.ndarray:
     """Per-site seeds of sweep color/strict: tagreset(rseed, id, 100) (src/app_lattice.cpp:287-295)."""
     return np.array([lib().spko_park_reset(rseed, i + 1, 100) for i in range(n)], dtype=np.int32)
+
+
+def bonds_sq4(spin2d: np.ndarray) -> int:
+    """Unlike nearest-neighbour bonds of a periodic square lattice, each once."""
+    s = spin2d
+    return int(np.sum(s != np.roll(s, -1, axis=1)) + np.sum(s != np.roll(s, -1, axis=0)))
+
+
+class EnsembleOracle:
+    """Restatement of the batched ensemble: every replica follows the oracle's
+    sq/4n colour sweep with Philox stream (r+1) << 8; every `every` sweeps the
+    replicas of equal L exchange temperatures between neighbouring slots
+    (sorted by T), slot pairs (j, j+1) with j = round mod 2, accepted when the
+    Philox word x of counter (round, group, j) satisfies
+    x < floor(exp((1/T_j - 1/T_j+1) (H_j - H_j+1)) 2^32) or the exponent is
+    >= 0; H = unlike bonds."""
+
+    def __init__(self, L, T, app="ising", nspins=2, seed=1, every=10):
+        import math
+
+        self.math = math
+        self.L = [int(v) for v in L]
+        self.T0 = [float(v) for v in T]
+        self.app, self.nspins, self.seed, self.every = app, nspins, seed, every
+        n = len(self.L)
+        order = sorted(range(n), key=lambda r: (self.L[r], self.T0[r], r))
+        self.groups = []
+        for r in order:
+            if not self.groups or self.L[self.groups[-1][0]] != self.L[r]:
+                self.groups.append([])
+            self.groups[-1].append(r)
+        self.slot_t = [list(g) for g in self.groups]
+        self.who = [list(g) for g in self.groups]
+        self.tidx = list(range(n))
+        self.sweep = 0
+        self.xround = 0
+        self.naccept = 0
+        self.tries = 0
+        self.accepts = 0
+        self.last_bonds = [0] * n
+
+    def run(self, spins: list, nsweeps: int):
+        for _ in range(nsweeps):
+            for r, sp in enumerate(spins):
+                cfg = make_cfg("sq/4n", self.L[r], self.L[r], 1, self.app, self.nspins, self.T0[self.tidx[r]],
+                               seed=self.seed, stream_base=(r + 1) << 8)
+                na, _, _ = color_sweeps(cfg, sp, self.sweep, 1)
+                self.naccept += na
+            self.sweep += 1
+            if self.every and self.sweep % self.every == 0:
+                bonds = [bonds_sq4(sp.reshape(self.L[r], self.L[r])) for r, sp in enumerate(spins)]
+                for g, (slots_t, who) in enumerate(zip(self.slot_t, self.who)):
+                    for j in range(self.xround & 1, len(who) - 1, 2):
+                        ra, rb = who[j], who[j + 1]
+                        ta, tb = slots_t[j], slots_t[j + 1]
+                        delta = (1.0 / self.T0[ta] - 1.0 / self.T0[tb]) * (float(bonds[ra]) - float(bonds[rb]))
+                        x = philox([self.xround, g, j, 0], [self.seed & 0xFFFFFFFF, 2])[0]
+                        ok = delta >= 0.0 or float(x) < self.math.floor(self.math.exp(delta) * 4294967296.0)
+                        self.tries += 1
+                        if ok:
+                            who[j], who[j + 1] = rb, ra
+                            self.tidx[ra], self.tidx[rb] = tb, ta
+                            self.accepts += 1
+                self.last_bonds = bonds
+                self.xround += 1
+
+    def temperatures(self):
+        return [self.T0[t] for t in self.tidx]

@@ -10,9 +10,12 @@
    known-answer vectors.
 
    Draw contract (the oracle and the GPU path must agree on it):
-     key      = { (uint32) seed, stream }
+     key      = { (uint32) seed, stream_base | stream }
      stream   0 = rejection sweeps, 1 = KMC events, 2 = replica exchange,
-              3 = initial spins
+              3 = initial spins; stream_base = 0 for a single lattice and
+              (r+1) << 8 for replica r of an ensemble
+     replica exchange round k, group g, slot pair j:
+       counter = { k, g, j, 0 }, word 0
      rejection sweep, site s = id-1 (0-based), sweep n, pass p within sweep:
        counter = { s>>1 (low 32), s>>33, n, p }, draw d of site s uses
        word 2*(s&1)+d  (two sites share one Philox block; d is 0 or 1)
@@ -57,10 +60,10 @@ static inline void spko_philox4x32_10(const uint32_t ctr[4], const uint32_t key[
 }
 
 /* the two draws of site s in sweep n, pass p */
-static inline void spko_site_draws(uint32_t seed, uint64_t s, uint32_t sweep, uint32_t pass,
-                                   uint32_t *x0, uint32_t *x1) {
+static inline void spko_site_draws(uint32_t seed, uint32_t stream_base, uint64_t s, uint32_t sweep,
+                                   uint32_t pass, uint32_t *x0, uint32_t *x1) {
   uint32_t ctr[4] = {(uint32_t)(s >> 1), (uint32_t)(s >> 33), sweep, pass};
-  uint32_t key[2] = {seed, SPKO_STREAM_SWEEP};
+  uint32_t key[2] = {seed, stream_base | SPKO_STREAM_SWEEP};
   uint32_t w[4];
   spko_philox4x32_10(ctr, key, w);
   int h = (int)(s & 1) * 2;

@@ -314,11 +314,10 @@ static int boltzmann_accept(double einitial, double efinal, double temperature, 
    potts           src/app_potts.cpp:112-146
    potts/neighonly src/app_potts_neighonly.cpp:71-117
    potts/neigh     src/app_potts_neigh.cpp:71-116
+   nb holds the site's neighbours (AppLattice::neighbor[i]).
    returns 1 if the spin changed */
-static int site_event_rejection(const spko_cfg *c, int32_t *spin, int64_t i, draw_src *d,
-                                uint8_t *mask) {
-  int64_t nb[26];
-  int nn = spko_neighbors(c, i, nb);
+static int site_event_rejection_nb(const spko_cfg *c, int32_t *spin, int64_t i, const int64_t *nb, int nn,
+                                   draw_src *d, uint8_t *mask) {
   int oldstate = spin[i];
   double einitial = site_energy(spin, i, nb, nn);
   int unique[27];
@@ -363,6 +362,12 @@ static int site_event_rejection(const spko_cfg *c, int32_t *spin, int64_t i, dra
   return spin[i] != oldstate;
 }
 
+static int site_event_rejection(const spko_cfg *c, int32_t *spin, int64_t i, draw_src *d, uint8_t *mask) {
+  int64_t nb[26];
+  int nn = spko_neighbors(c, i, nb);
+  return site_event_rejection_nb(c, spin, i, nb, nn, d, mask);
+}
+
 /* ---------------------------------------------------------------------- */
 /* colour sweeps: AppLattice::iterate_rejection (src/app_lattice.cpp:632-711)
    with sweep color / color/strict; sets are colours, or sectors x colours
@@ -384,66 +389,78 @@ int spko_color_sweeps(const spko_cfg *c, int32_t *spin, int64_t sweep0, int nswe
   int nsec = c->nsector > 1 ? c->nsector : 1;
   int nloop = c->nloop > 0 ? c->nloop : 1;
   int nprocs = (c->px > 0 ? c->px : 1) * (c->py > 0 ? c->py : 1) * (c->pz > 0 ? c->pz : 1);
+  int nn = spko_maxneigh(c->lattice);
   if (c->rng == SPKO_RNG_STRICT && !siteseeds) return -1;
-  /* per-site set membership, precomputed */
-  int *col = (int *)malloc(sizeof(int) * n);
-  int *sec = (int *)malloc(sizeof(int) * n);
-  int *prc = (int *)malloc(sizeof(int) * n);
+  /* the reference's own layout: neighbor[i][j] and one ascending site list
+     per (sector, colour, processor) set (AppLattice::create_set) */
+  int64_t *nbt = (int64_t *)malloc(sizeof(int64_t) * n * nn);
+  int nsets = nsec * ncol * nprocs;
+  int64_t *count = (int64_t *)calloc((size_t)nsets + 1, sizeof(int64_t));
+  int *setof = (int *)malloc(sizeof(int) * n);
   for (int64_t i = 0; i < n; i++) {
-    col[i] = spko_color(c, i);
-    sec[i] = spko_sector(c, i);
-    prc[i] = proc_index(c, i);
+    spko_neighbors(c, i, nbt + i * nn);
+    int k = ((spko_sector(c, i) - 1) * ncol + (spko_color(c, i) - 1)) * nprocs + proc_index(c, i);
+    setof[i] = k;
+    count[k + 1]++;
   }
+  for (int k = 0; k < nsets; k++) count[k + 1] += count[k];
+  int64_t *lists = (int64_t *)malloc(sizeof(int64_t) * (n + 1));
+  int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (nsets + 1));
+  memcpy(fill, count, sizeof(int64_t) * (nsets + 1));
+  for (int64_t i = 0; i < n; i++) lists[fill[setof[i]]++] = i;
   for (int s = 0; s < nsweeps; s++) {
     uint32_t sweep = (uint32_t)(sweep0 + s);
     for (int isec = 1; isec <= nsec; isec++) {
       /* with a mask, clear it on the border sites of the set about to be
          swept (AppLattice::boundary_clear_mask, src/app_lattice.cpp:1157) */
-      if (mask) {
+      if (mask && nsec > 1) {
         for (int64_t i = 0; i < n; i++) {
-          if (nsec > 1) {
-            if (sec[i] != isec) continue;
-            int64_t nb[26];
-            int nn = spko_neighbors(c, i, nb);
-            for (int j = 0; j < nn; j++)
-              if (!in_same_set(c, i, nb[j])) {
-                mask[i] = 0;
-                break;
-              }
-          }
+          if (spko_sector(c, i) != isec) continue;
+          for (int j = 0; j < nn; j++)
+            if (!in_same_set(c, i, nbt[i * nn + j])) {
+              mask[i] = 0;
+              break;
+            }
         }
       }
       for (int icol = 1; icol <= ncol; icol++) {
-        if (mask && nsec == 1) {
+        int64_t setsize = 0;
+        for (int proc = 0; proc < nprocs; proc++) {
+          int k = ((isec - 1) * ncol + (icol - 1)) * nprocs + proc;
+          setsize += count[k + 1] - count[k];
           /* colour sets: every site borders another set */
-          for (int64_t i = 0; i < n; i++)
-            if (col[i] == icol) mask[i] = 0;
+          if (mask && nsec == 1)
+            for (int64_t m = count[k]; m < count[k + 1]; m++) mask[lists[m]] = 0;
         }
         for (int p = 0; p < nloop; p++) {
-          for (int proc = 0; proc < nprocs; proc++)
-            for (int64_t i = 0; i < n; i++) {
-              if (col[i] != icol || sec[i] != isec || prc[i] != proc) continue;
+          for (int proc = 0; proc < nprocs; proc++) {
+            int k = ((isec - 1) * ncol + (icol - 1)) * nprocs + proc;
+            for (int64_t m = count[k]; m < count[k + 1]; m++) {
+              int64_t i = lists[m];
               if (mask && mask[i]) continue;
               draw_src d;
               d.mode = c->rng;
               d.used = 0;
               d.park = siteseeds ? &siteseeds[i] : NULL;
               if (c->rng == SPKO_RNG_PHILOX)
-                spko_site_draws(c->seed, (uint64_t)i, sweep, (uint32_t)p, &d.x[0], &d.x[1]);
-              *naccept += site_event_rejection(c, spin, i, &d, mask);
+                spko_site_draws(c->seed, c->stream_base, (uint64_t)i, sweep, (uint32_t)p, &d.x[0],
+                                &d.x[1]);
+              *naccept += site_event_rejection_nb(c, spin, i, nbt + i * nn, nn, &d, mask);
             }
+          }
         }
         /* nattempt counts every site of the set, masked or not
            (src/app_lattice.cpp:690) */
-        for (int64_t i = 0; i < n; i++)
-          if (col[i] == icol && sec[i] == isec) *nattempt += nloop;
+        *nattempt += setsize * nloop;
       }
     }
     if (hashes) hashes[s] = spko_hash(spin, n);
   }
-  free(col);
-  free(sec);
-  free(prc);
+  free(nbt);
+  free(count);
+  free(setof);
+  free(lists);
+  free(fill);
   return 0;
 }
 

@@ -30,6 +30,8 @@ typedef struct {
   uint32_t seed;        /* Philox key word 0 */
   int mask;             /* sweep ... mask yes */
   int px, py, pz;       /* processor grid (1 1 1 = serial) */
+  uint32_t stream_base; /* Philox key word 1 = stream_base | stream; replica r
+                           of an ensemble uses (r+1) << 8 */
 } spko_cfg;
 
 int spko_maxneigh(int lattice);

@@ -58,6 +58,7 @@ class Desc(ctypes.Structure):
         ("mask", ctypes.c_int32),
         ("seed", ctypes.c_uint32),
         ("device", ctypes.c_int32),
+        ("variant", ctypes.c_int32),
     ]
 
 
@@ -70,6 +71,24 @@ class KmcStats(ctypes.Structure):
                 ("dt_kmc", ctypes.c_double), ("total_propensity", ctypes.c_double)]
 
 
+class EnsembleDesc(ctypes.Structure):
+    _fields_ = [
+        ("nreplica", ctypes.c_int32),
+        ("L", ctypes.POINTER(ctypes.c_int32)),
+        ("temperature", ctypes.POINTER(ctypes.c_double)),
+        ("app", ctypes.c_int32),
+        ("nspins", ctypes.c_int32),
+        ("seed", ctypes.c_uint32),
+        ("exchange_every", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+    ]
+
+
+class EnsembleStats(ctypes.Structure):
+    _fields_ = [("naccept", ctypes.c_int64), ("nattempt", ctypes.c_int64), ("nsweeps", ctypes.c_int64),
+                ("exchange_tries", ctypes.c_int64), ("exchange_accepts", ctypes.c_int64)]
+
+
 # every symbol include/spkgpu.h (and the other include/*.h) declares
 EXPORTS = [
     "spkgpu_create", "spkgpu_destroy", "spkgpu_last_error", "spkgpu_version", "spkgpu_set_temperature",
@@ -77,6 +96,10 @@ EXPORTS = [
     "spkgpu_upload_mask", "spkgpu_download_mask", "spkgpu_sweep", "spkgpu_set_sweep_index",
     "spkgpu_get_stats", "spkgpu_energy", "spkgpu_synchronize", "spkgpu_timed_sweeps", "spkgpu_stream",
     "spkgpu_device_spins", "spkgpu_launch_count", "spkgpu_kmc_setup", "spkgpu_kmc_run",
+    "spkgpu_ensemble_create", "spkgpu_ensemble_destroy", "spkgpu_ensemble_last_error", "spkgpu_ensemble_upload",
+    "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
+    "spkgpu_ensemble_get_stats", "spkgpu_ensemble_temperatures", "spkgpu_ensemble_energies",
+    "spkgpu_ensemble_launch_count",
 ]
 
 _lib = None
@@ -114,6 +137,19 @@ def load_library(path: Path | None = None):
     L.spkgpu_launch_count.argtypes = [vp, P(ctypes.c_int64)]
     L.spkgpu_kmc_setup.argtypes = [vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32]
     L.spkgpu_kmc_run.argtypes = [vp, P(ctypes.c_double), ctypes.c_double, P(KmcStats)]
+    L.spkgpu_ensemble_create.argtypes = [P(EnsembleDesc), P(vp)]
+    L.spkgpu_ensemble_destroy.argtypes = [vp]
+    L.spkgpu_ensemble_last_error.argtypes = [vp]
+    L.spkgpu_ensemble_last_error.restype = ctypes.c_char_p
+    L.spkgpu_ensemble_upload.argtypes = [vp, P(ctypes.c_int32), ctypes.c_int64]
+    L.spkgpu_ensemble_download.argtypes = [vp, P(ctypes.c_int32), ctypes.c_int64]
+    L.spkgpu_ensemble_run.argtypes = [vp, ctypes.c_int32]
+    L.spkgpu_ensemble_timed_run.argtypes = [vp, ctypes.c_int32, P(ctypes.c_float)]
+    L.spkgpu_ensemble_synchronize.argtypes = [vp]
+    L.spkgpu_ensemble_get_stats.argtypes = [vp, P(EnsembleStats)]
+    L.spkgpu_ensemble_temperatures.argtypes = [vp, P(ctypes.c_double)]
+    L.spkgpu_ensemble_energies.argtypes = [vp, P(ctypes.c_int64)]
+    L.spkgpu_ensemble_launch_count.argtypes = [vp, P(ctypes.c_int64)]
     if path is None:
         _lib = L
     return L
@@ -127,7 +163,7 @@ class Lattice:
     """One lattice on the GPU behind the C ABI."""
 
     def __init__(self, lattice="sq/4n", nx=16, ny=16, nz=1, app="ising", nspins=2, spin_bytes=0, nsector=1,
-                 nloop=1, procs=(1, 1, 1), rng=RNG_PHILOX, mask=False, seed=12345, device=0):
+                 nloop=1, procs=(1, 1, 1), rng=RNG_PHILOX, mask=False, seed=12345, device=0, variant=0):
         self.lib = load_library()
         d = Desc()
         d.lattice = LATTICE_STYLES[lattice] if isinstance(lattice, str) else int(lattice)
@@ -142,6 +178,7 @@ class Lattice:
         d.mask = int(bool(mask))
         d.seed = seed & 0xFFFFFFFF
         d.device = device
+        d.variant = variant
         self.desc = d
         self.n = nx * ny * nz
         self.h = ctypes.c_void_p()
@@ -235,3 +272,88 @@ class Lattice:
         self._check(self.lib.spkgpu_kmc_run(self.h, ctypes.byref(t), float(stoptime), ctypes.byref(s)))
         return {"time": s.time, "naccept": s.naccept, "npass": s.npass, "dt_kmc": s.dt_kmc,
                 "total_propensity": s.total_propensity}
+
+
+class Ensemble:
+    """Batched sq/4n replicas of uneven size and temperature with on-device
+    replica exchange (spkgpu_ensemble_* in include/spkgpu.h)."""
+
+    def __init__(self, L, temperature, app="ising", nspins=2, seed=12345, exchange_every=10, device=0):
+        self.lib = load_library()
+        self.L = np.ascontiguousarray(L, dtype=np.int32)
+        self.T = np.ascontiguousarray(temperature, dtype=np.float64)
+        d = EnsembleDesc()
+        d.nreplica = len(self.L)
+        d.L = self.L.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        d.temperature = self.T.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.app = APP_STYLES[app] if isinstance(app, str) else int(app)
+        d.nspins = nspins
+        d.seed = seed & 0xFFFFFFFF
+        d.exchange_every = exchange_every
+        d.device = device
+        self.nsites = int(np.sum(self.L.astype(np.int64) ** 2))
+        self.offsets = np.concatenate([[0], np.cumsum(self.L.astype(np.int64) ** 2)])
+        self.h = ctypes.c_void_p()
+        rc = self.lib.spkgpu_ensemble_create(ctypes.byref(d), ctypes.byref(self.h))
+        if rc != 0:
+            self.h = None
+            raise SpkGpuError(rc, "spkgpu_ensemble_create rejected the ensemble description")
+
+    def _check(self, rc):
+        if rc != 0:
+            raise SpkGpuError(rc, self.lib.spkgpu_ensemble_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.spkgpu_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, spin):
+        s = np.ascontiguousarray(spin, dtype=np.int32)
+        self._check(self.lib.spkgpu_ensemble_upload(self.h, _i32p(s), s.size))
+
+    def download(self, out=None):
+        out = np.empty(self.nsites, dtype=np.int32) if out is None else out
+        self._check(self.lib.spkgpu_ensemble_download(self.h, _i32p(out), out.size))
+        return out
+
+    def replica(self, spin, r):
+        return spin[self.offsets[r]:self.offsets[r + 1]]
+
+    def run(self, nsweeps):
+        self._check(self.lib.spkgpu_ensemble_run(self.h, int(nsweeps)))
+
+    def timed_run(self, nsweeps) -> float:
+        ms = ctypes.c_float()
+        self._check(self.lib.spkgpu_ensemble_timed_run(self.h, int(nsweeps), ctypes.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        self._check(self.lib.spkgpu_ensemble_synchronize(self.h))
+
+    def stats(self) -> dict:
+        s = EnsembleStats()
+        self._check(self.lib.spkgpu_ensemble_get_stats(self.h, ctypes.byref(s)))
+        return {"naccept": s.naccept, "nattempt": s.nattempt, "nsweeps": s.nsweeps,
+                "exchange_tries": s.exchange_tries, "exchange_accepts": s.exchange_accepts}
+
+    def temperatures(self) -> np.ndarray:
+        out = np.empty(len(self.L), dtype=np.float64)
+        self._check(self.lib.spkgpu_ensemble_temperatures(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def energies(self) -> np.ndarray:
+        out = np.empty(len(self.L), dtype=np.int64)
+        self._check(self.lib.spkgpu_ensemble_energies(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return out
+
+    def launch_count(self) -> int:
+        c = ctypes.c_int64()
+        self._check(self.lib.spkgpu_ensemble_launch_count(self.h, ctypes.byref(c)))
+        return c.value

@@ -24,6 +24,7 @@ SOURCES = [
     "sweep_generic.cu",
     "sweep_fused2d.cu",
     "kmc.cu",
+    "ensemble.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

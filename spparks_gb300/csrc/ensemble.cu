@@ -1,0 +1,585 @@
+// Batched ensemble: hundreds of independent sq/4n lattices of uneven size and
+// temperature swept by one persistent cooperative kernel per step, with
+// parallel-tempering replica exchange on the device, replayed from a
+// captured CUDA graph.
+//
+// Each sweep every CTA takes 32x32 tiles of all replicas round-robin and runs
+// tile_sweep_sq4 (both colours of the sweep, double-buffered); a bounded grid
+// barrier separates sweeps.  Every exchange_every sweeps the kernel counts the
+// unlike bonds of each replica, then one thread walks the exchange pairs:
+// replicas of equal L form a group whose temperature slots are sorted
+// ascending; round k tries slot pairs (j, j+1) with j = k mod 2 and accepts
+// with probability min(1, exp((1/T_j - 1/T_j+1) (H_j - H_j+1))), H = bonds.
+// An accepted exchange swaps the two replicas' temperatures.
+//
+// The reference has no ensemble (one AppLattice per process); per replica
+// the update rule is exactly that of `sweep color` on sq/4n.
+
+#include <cuda/atomic>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "spk_internal.h"
+#include "tile_sweep.cuh"
+
+namespace spk {
+
+// device control block of an ensemble
+struct EnsCtl {
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int err;
+  int parity;                   // buffer holding the current state
+  uint32_t sweep;               // next sweep index
+  uint32_t xround;              // next exchange round
+  unsigned long long naccept;
+  unsigned long long xtries;
+  unsigned long long xaccepts;
+};
+
+struct EnsArgs {
+  void *buf0, *buf1;
+  const int32_t *L;
+  const int64_t *base;
+  const int32_t *tile_start;    // nrep+1 prefix of tiles per replica
+  int nrep, ntiles;
+  int32_t *tidx;                // replica -> temperature index
+  const uint64_t *thr;          // [ntemp][5]
+  const double *beta;           // [ntemp]
+  const int32_t *group_start;   // ngroups+1 prefix of slots
+  const int32_t *slot_t;        // temperature index of each slot (ascending T)
+  int32_t *who;                 // replica in each slot
+  unsigned long long *bonds;    // per replica, accumulated at an exchange
+  long long *last_bonds;        // per replica, copy at the last exchange
+  int ngroups;
+  int nsweeps;
+  int exchange_every;
+  int nspins;
+  uint32_t seed;
+  EnsCtl *ctl;
+};
+
+constexpr long long kBarrierSpinLimit = 1LL << 25;  // ~seconds with nanosleep: then give up
+
+// grid-wide barrier for a cooperative launch, bounded: a block that waits
+// too long sets ctl->err and stops waiting; callers then leave the kernel.
+// Arrival is a release RMW and the wait an acquire load at device scope, so
+// the writes of every block before the barrier (spins, temperatures) are
+// visible to every block after it.
+__device__ bool grid_barrier(EnsCtl *ctl) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<unsigned int, cuda::thread_scope_device> gen(ctl->bar_gen);
+    cuda::atomic_ref<unsigned int, cuda::thread_scope_device> count(ctl->bar_count);
+    cuda::atomic_ref<int, cuda::thread_scope_device> err(ctl->err);
+    unsigned int my = gen.load(cuda::memory_order_acquire);
+    unsigned int arrived = count.fetch_add(1u, cuda::memory_order_acq_rel);
+    if (arrived == gridDim.x - 1) {
+      count.store(0u, cuda::memory_order_relaxed);
+      gen.fetch_add(1u, cuda::memory_order_acq_rel);
+    } else {
+      long long it = 0;
+      while (gen.load(cuda::memory_order_acquire) == my) {
+        if (++it > kBarrierSpinLimit || err.load(cuda::memory_order_relaxed)) {
+          err.store(1, cuda::memory_order_relaxed);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+  }
+  __syncthreads();
+  return *(volatile int *)&ctl->err == 0;
+}
+
+__device__ __forceinline__ int replica_of_tile(const int32_t *tile_start, int nrep, int t) {
+  int lo = 0, hi = nrep;  // largest r with tile_start[r] <= t
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (tile_start[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int APP, typename S>
+__global__ void __launch_bounds__(kTileThreads) ensemble_kernel(EnsArgs a) {
+  __shared__ S stage[kStage * kStage];
+  __shared__ uint64_t thr[5];
+  __shared__ unsigned long long red[kTileThreads / 32];
+  EnsCtl *ctl = a.ctl;
+  int parity = *(volatile int *)&ctl->parity;
+  uint32_t sweep0 = *(volatile uint32_t *)&ctl->sweep;
+  uint32_t xround = *(volatile uint32_t *)&ctl->xround;
+  unsigned long long my_changed = 0;
+  bool ok = true;
+  for (int s = 0; s < a.nsweeps && ok; s++) {
+    const void *src = parity ? a.buf1 : a.buf0;
+    void *dst = parity ? a.buf0 : a.buf1;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+      int r = replica_of_tile(a.tile_start, a.nrep, t);
+      int L = a.L[r];
+      int tpr = L / kTile;
+      int lt = t - a.tile_start[r];
+      if (threadIdx.x < 5) thr[threadIdx.x] = a.thr[(int64_t)a.tidx[r] * 5 + threadIdx.x];
+      TileJob j;
+      j.src = (const S *)src + a.base[r];
+      j.dst = (S *)dst + a.base[r];
+      j.L = L;
+      j.Ly = L;
+      j.x0 = (lt % tpr) * kTile;
+      j.y0 = (lt / tpr) * kTile;
+      j.base = a.base[r];
+      j.seed = a.seed;
+      j.key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
+      j.sweep = sweep0 + (uint32_t)s;
+      j.nspins = a.nspins;
+      j.zero_t = 0;
+      j.thr = thr;
+      my_changed += (unsigned long long)tile_sweep_sq4<APP, S>(j, stage);
+    }
+    parity ^= 1;
+    ok = grid_barrier(ctl);
+    if (!ok) break;
+    uint32_t done = sweep0 + (uint32_t)s + 1;
+    if (a.exchange_every > 0 && done % (uint32_t)a.exchange_every == 0) {
+      // unlike bonds of each replica (right and down neighbour of each site)
+      const S *cur = (const S *)(parity ? a.buf1 : a.buf0);
+      for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        int r = replica_of_tile(a.tile_start, a.nrep, t);
+        int L = a.L[r];
+        int tpr = L / kTile;
+        int lt = t - a.tile_start[r];
+        int x0 = (lt % tpr) * kTile, y0 = (lt / tpr) * kTile;
+        const S *rep = cur + a.base[r];
+        unsigned int b = 0;
+        for (int k = threadIdx.x; k < kTile * kTile; k += kTileThreads) {
+          int y = y0 + (k >> 5), x = x0 + (k & 31);
+          S v = rep[(int64_t)y * L + x];
+          int xr = x + 1 == L ? 0 : x + 1;
+          int yd = y + 1 == L ? 0 : y + 1;
+          b += (rep[(int64_t)y * L + xr] != v) + (rep[(int64_t)yd * L + x] != v);
+        }
+        unsigned int w = __reduce_add_sync(0xFFFFFFFFu, b);
+        if ((threadIdx.x & 31) == 0 && w) atomicAdd(&a.bonds[r], (unsigned long long)w);
+      }
+      ok = grid_barrier(ctl);
+      if (!ok) break;
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        unsigned long long tries = 0, acc = 0;
+        for (int g = 0; g < a.ngroups; g++) {
+          int lo = a.group_start[g], hi = a.group_start[g + 1];
+          for (int jj = lo + (int)(xround & 1u); jj + 1 < hi; jj += 2) {
+            int ra = a.who[jj], rb = a.who[jj + 1];
+            int ta = a.slot_t[jj], tb = a.slot_t[jj + 1];
+            double delta = (a.beta[ta] - a.beta[tb]) * ((double)a.bonds[ra] - (double)a.bonds[rb]);
+            U4 w = philox4x32_10(U4{xround, (uint32_t)g, (uint32_t)(jj - lo), 0u}, a.seed, kStreamExchange);
+            bool accept = delta >= 0.0;
+            if (!accept) {
+              double p = exp(delta) * 4294967296.0;
+              accept = (double)w.x < floor(p);
+            }
+            tries++;
+            if (accept) {
+              a.who[jj] = rb;
+              a.who[jj + 1] = ra;
+              a.tidx[ra] = tb;
+              a.tidx[rb] = ta;
+              acc++;
+            }
+          }
+        }
+        for (int r = 0; r < a.nrep; r++) {
+          a.last_bonds[r] = (long long)a.bonds[r];
+          a.bonds[r] = 0;
+        }
+        ctl->xtries += tries;
+        ctl->xaccepts += acc;
+        __threadfence();
+      }
+      xround++;
+      ok = grid_barrier(ctl);
+    }
+  }
+  unsigned long long w = my_changed;
+  for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xFFFFFFFFu, w, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = w;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int k = 0; k < kTileThreads / 32; k++) tot += red[k];
+    if (tot) atomicAdd(&ctl->naccept, tot);
+  }
+  ok = grid_barrier(ctl) && ok;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && ok) {
+    ctl->parity = parity;
+    ctl->sweep = sweep0 + (uint32_t)a.nsweeps;
+    ctl->xround = xround;
+  }
+}
+
+template <int APP, typename S>
+static void *ensemble_fn() {
+  return (void *)ensemble_kernel<APP, S>;
+}
+
+}  // namespace spk
+
+using namespace spk;
+
+struct spkgpu_ensemble {
+  spkgpu_ensemble_desc d;
+  std::vector<int32_t> L;
+  std::vector<double> T0;
+  std::vector<int64_t> base;
+  int64_t nsites = 0;
+  int ntiles = 0;
+  int spin_bytes = 1;
+  int num_sms = 1;
+  int grid = 1;
+  int chunk = 10;
+  void *kfn = nullptr;
+  void *buf[2] = {nullptr, nullptr};
+  int32_t *d_L = nullptr, *d_tile_start = nullptr, *d_tidx = nullptr, *d_group_start = nullptr,
+          *d_slot_t = nullptr, *d_who = nullptr;
+  int64_t *d_base = nullptr;
+  uint64_t *d_thr = nullptr;
+  double *d_beta = nullptr;
+  unsigned long long *d_bonds = nullptr;
+  long long *d_last_bonds = nullptr;
+  EnsCtl *d_ctl = nullptr;
+  int32_t *d_stage = nullptr;
+  int *d_bad = nullptr;
+  int ngroups = 0;
+  int parity = 0;
+  int64_t nsweeps_done = 0;
+  int64_t launches = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  EnsArgs args;
+  std::string err;
+};
+
+static int ens_fail(spkgpu_ensemble *e, int code, const std::string &m) {
+  if (e) e->err = m;
+  return code;
+}
+
+static int ens_cuda(spkgpu_ensemble *e, cudaError_t c, const char *what) {
+  return ens_fail(e, SPKGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(c));
+}
+
+#define ENS_CUDA(e, call)                                   \
+  do {                                                      \
+    cudaError_t c__ = (call);                               \
+    if (c__ != cudaSuccess) return ens_cuda(e, c__, #call); \
+  } while (0)
+
+static cudaError_t ens_launch(spkgpu_ensemble *e, int nsweeps) {
+  EnsArgs a = e->args;
+  a.nsweeps = nsweeps;
+  void *params[] = {&a};
+  return cudaLaunchCooperativeKernel(e->kfn, dim3(e->grid), dim3(kTileThreads), params, 0, e->stream);
+}
+
+extern "C" {
+
+const char *spkgpu_ensemble_last_error(const spkgpu_ensemble *e) { return e ? e->err.c_str() : "null handle"; }
+
+int spkgpu_ensemble_destroy(spkgpu_ensemble *e) {
+  if (!e) return SPKGPU_ERR_ARG;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  cudaFree(e->buf[0]);
+  cudaFree(e->buf[1]);
+  cudaFree(e->d_L);
+  cudaFree(e->d_tile_start);
+  cudaFree(e->d_tidx);
+  cudaFree(e->d_group_start);
+  cudaFree(e->d_slot_t);
+  cudaFree(e->d_who);
+  cudaFree(e->d_base);
+  cudaFree(e->d_thr);
+  cudaFree(e->d_beta);
+  cudaFree(e->d_bonds);
+  cudaFree(e->d_last_bonds);
+  cudaFree(e->d_ctl);
+  cudaFree(e->d_stage);
+  cudaFree(e->d_bad);
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **out) {
+  if (!desc || !out || !desc->L || !desc->temperature) return SPKGPU_ERR_ARG;
+  *out = nullptr;
+  const spkgpu_ensemble_desc &d = *desc;
+  if (d.nreplica <= 0 || d.nreplica > (1 << 20)) return SPKGPU_ERR_ARG;
+  if (d.app != SPKGPU_ISING && d.app != SPKGPU_POTTS) return SPKGPU_ERR_ARG;
+  if (d.app == SPKGPU_ISING && d.nspins != 2) return SPKGPU_ERR_ARG;
+  if (d.nspins < 1 || d.nspins > 127) return SPKGPU_ERR_ARG;
+  if (d.exchange_every < 0) return SPKGPU_ERR_ARG;
+  for (int r = 0; r < d.nreplica; r++) {
+    if (d.L[r] < kTile || d.L[r] % kTile || d.L[r] > (1 << 16)) return SPKGPU_ERR_ARG;
+    if (!(d.temperature[r] > 0.0) || isinf(d.temperature[r])) return SPKGPU_ERR_ARG;
+  }
+  spkgpu_ensemble *e = new (std::nothrow) spkgpu_ensemble();
+  if (!e) return SPKGPU_ERR_NOMEM;
+  e->d = d;
+  e->L.assign(d.L, d.L + d.nreplica);
+  e->T0.assign(d.temperature, d.temperature + d.nreplica);
+  e->d.L = nullptr;
+  e->d.temperature = nullptr;
+  auto fail = [&](int c) {
+    spkgpu_ensemble_destroy(e);
+    return c;
+  };
+  if (cudaSetDevice(d.device) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
+  cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, d.device);
+  int n = d.nreplica;
+  std::vector<int32_t> tile_start(n + 1, 0);
+  e->base.resize(n);
+  int64_t off = 0;
+  for (int r = 0; r < n; r++) {
+    e->base[r] = off;
+    off += (int64_t)e->L[r] * e->L[r];
+    tile_start[r + 1] = tile_start[r] + (e->L[r] / kTile) * (e->L[r] / kTile);
+  }
+  e->nsites = off;
+  e->ntiles = tile_start[n];
+  // temperatures: index t = the replica that started with it
+  std::vector<uint64_t> thr((size_t)n * 5);
+  std::vector<double> beta(n);
+  for (int t = 0; t < n; t++) {
+    AcceptTable at;
+    build_accept_table(e->T0[t], &at);
+    for (int k = 0; k < 5; k++) thr[(size_t)t * 5 + k] = at.thr[k];
+    beta[t] = 1.0 / e->T0[t];
+  }
+  // exchange groups: equal L, slots by ascending (T, replica)
+  std::vector<int32_t> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (e->L[a] != e->L[b]) return e->L[a] < e->L[b];
+    if (e->T0[a] != e->T0[b]) return e->T0[a] < e->T0[b];
+    return a < b;
+  });
+  std::vector<int32_t> group_start{0}, slot_t(n), who(n), tidx(n);
+  for (int k = 0; k < n; k++) {
+    if (k > 0 && e->L[order[k]] != e->L[order[k - 1]]) group_start.push_back(k);
+    slot_t[k] = order[k];
+    who[k] = order[k];
+  }
+  group_start.push_back(n);
+  e->ngroups = (int)group_start.size() - 1;
+  std::iota(tidx.begin(), tidx.end(), 0);
+
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
+  if (cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
+  auto dmalloc = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes == 0 ? 16 : bytes) == cudaSuccess; };
+  size_t sb = (size_t)e->spin_bytes;
+  if (!dmalloc(&e->buf[0], e->nsites * sb) || !dmalloc(&e->buf[1], e->nsites * sb) ||
+      !dmalloc((void **)&e->d_L, n * 4) || !dmalloc((void **)&e->d_tile_start, (n + 1) * 4) ||
+      !dmalloc((void **)&e->d_tidx, n * 4) || !dmalloc((void **)&e->d_group_start, group_start.size() * 4) ||
+      !dmalloc((void **)&e->d_slot_t, n * 4) || !dmalloc((void **)&e->d_who, n * 4) ||
+      !dmalloc((void **)&e->d_base, n * 8) || !dmalloc((void **)&e->d_thr, thr.size() * 8) ||
+      !dmalloc((void **)&e->d_beta, n * 8) || !dmalloc((void **)&e->d_bonds, n * 8) ||
+      !dmalloc((void **)&e->d_last_bonds, n * 8) || !dmalloc((void **)&e->d_ctl, sizeof(EnsCtl)) ||
+      !dmalloc((void **)&e->d_bad, sizeof(int)))
+    return fail(SPKGPU_ERR_NOMEM);
+  cudaMemcpy(e->d_L, e->L.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_tile_start, tile_start.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_tidx, tidx.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_group_start, group_start.data(), group_start.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_slot_t, slot_t.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_who, who.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_base, e->base.data(), n * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_thr, thr.data(), thr.size() * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_beta, beta.data(), n * 8, cudaMemcpyHostToDevice);
+  cudaMemset(e->d_bonds, 0, n * 8);
+  cudaMemset(e->d_last_bonds, 0, n * 8);
+  cudaMemset(e->d_ctl, 0, sizeof(EnsCtl));
+  cudaMemset(e->buf[0], 0, e->nsites * sb);
+  cudaMemset(e->buf[1], 0, e->nsites * sb);
+  e->kfn = (d.app == SPKGPU_ISING) ? ensemble_fn<SPKGPU_ISING, int8_t>() : ensemble_fn<SPKGPU_POTTS, int8_t>();
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e->kfn, kTileThreads, 0) != cudaSuccess || per_sm < 1)
+    return fail(ens_cuda(e, cudaGetLastError(), "occupancy query"));
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, d.device);
+  if (!coop) return fail(ens_fail(e, SPKGPU_ERR_UNSUPPORTED, "device lacks cooperative launch"));
+  e->grid = std::min(e->ntiles, per_sm * e->num_sms);
+  e->chunk = d.exchange_every > 0 ? d.exchange_every : 10;
+  EnsArgs &a = e->args;
+  a.buf0 = e->buf[0];
+  a.buf1 = e->buf[1];
+  a.L = e->d_L;
+  a.base = e->d_base;
+  a.tile_start = e->d_tile_start;
+  a.nrep = n;
+  a.ntiles = e->ntiles;
+  a.tidx = e->d_tidx;
+  a.thr = e->d_thr;
+  a.beta = e->d_beta;
+  a.group_start = e->d_group_start;
+  a.slot_t = e->d_slot_t;
+  a.who = e->d_who;
+  a.bonds = e->d_bonds;
+  a.last_bonds = e->d_last_bonds;
+  a.ngroups = e->ngroups;
+  a.nsweeps = 0;
+  a.exchange_every = d.exchange_every;
+  a.nspins = d.nspins;
+  a.seed = d.seed;
+  a.ctl = e->d_ctl;
+  if (cudaDeviceSynchronize() != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
+  // capture one step (chunk sweeps) as a graph; replayed by spkgpu_ensemble_run
+  cudaStream_t cap = e->stream;
+  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    cudaError_t le = ens_launch(e, e->chunk);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    if (le == cudaSuccess && ce == cudaSuccess && g &&
+        cudaGraphInstantiate(&e->gexec, g, 0) == cudaSuccess) {
+      e->graph = g;
+    } else {
+      if (g) cudaGraphDestroy(g);
+      e->gexec = nullptr;
+      cudaGetLastError();  // capture unsupported: launch directly instead
+    }
+  }
+  *out = e;
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_upload(spkgpu_ensemble *e, const int32_t *spin, int64_t n) {
+  if (!e || !spin) return SPKGPU_ERR_ARG;
+  if (n != e->nsites) return ens_fail(e, SPKGPU_ERR_ARG, "site count mismatch");
+  const int64_t chunk = (int64_t)1 << 24;
+  if (!e->d_stage) ENS_CUDA(e, cudaMalloc(&e->d_stage, (size_t)std::min(chunk, n) * 4));
+  ENS_CUDA(e, cudaMemsetAsync(e->d_bad, 0, sizeof(int), e->stream));
+  for (int64_t off = 0; off < n; off += chunk) {
+    int64_t m = std::min(chunk, n - off);
+    ENS_CUDA(e, cudaMemcpyAsync(e->d_stage, spin + off, (size_t)m * 4, cudaMemcpyHostToDevice, e->stream));
+    ENS_CUDA(e, launch_convert_in(1, e->d_stage, (int8_t *)e->buf[e->parity] + off, m, e->d.nspins, e->d_bad,
+                                  e->stream));
+    e->launches++;
+  }
+  int bad = 0;
+  ENS_CUDA(e, cudaMemcpyAsync(&bad, e->d_bad, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  if (bad) return ens_fail(e, SPKGPU_ERR_INVALID_SPIN, "One or more sites have invalid values");
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_download(spkgpu_ensemble *e, int32_t *spin, int64_t n) {
+  if (!e || !spin) return SPKGPU_ERR_ARG;
+  if (n != e->nsites) return ens_fail(e, SPKGPU_ERR_ARG, "site count mismatch");
+  const int64_t chunk = (int64_t)1 << 24;
+  if (!e->d_stage) ENS_CUDA(e, cudaMalloc(&e->d_stage, (size_t)std::min(chunk, n) * 4));
+  for (int64_t off = 0; off < n; off += chunk) {
+    int64_t m = std::min(chunk, n - off);
+    ENS_CUDA(e, launch_convert_out(1, (const int8_t *)e->buf[e->parity] + off, e->d_stage, m, e->stream));
+    e->launches++;
+    ENS_CUDA(e, cudaMemcpyAsync(spin + off, e->d_stage, (size_t)m * 4, cudaMemcpyDeviceToHost, e->stream));
+  }
+  ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  return SPKGPU_OK;
+}
+
+static int ens_enqueue(spkgpu_ensemble *e, int32_t nsweeps) {
+  int32_t left = nsweeps;
+  while (left > 0) {
+    if (e->gexec && left >= e->chunk) {
+      ENS_CUDA(e, cudaGraphLaunch(e->gexec, e->stream));
+      left -= e->chunk;
+      e->parity ^= (e->chunk & 1);
+    } else {
+      int32_t m = std::min(left, e->chunk);
+      ENS_CUDA(e, ens_launch(e, m));
+      left -= m;
+      e->parity ^= (m & 1);
+    }
+    e->launches++;
+  }
+  e->nsweeps_done += nsweeps;
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_run(spkgpu_ensemble *e, int32_t nsweeps) {
+  if (!e || nsweeps < 0) return SPKGPU_ERR_ARG;
+  return ens_enqueue(e, nsweeps);
+}
+
+int spkgpu_ensemble_timed_run(spkgpu_ensemble *e, int32_t nsweeps, float *ms) {
+  if (!e || !ms || nsweeps < 0) return SPKGPU_ERR_ARG;
+  ENS_CUDA(e, cudaEventRecord(e->ev0, e->stream));
+  int rc = ens_enqueue(e, nsweeps);
+  if (rc) return rc;
+  ENS_CUDA(e, cudaEventRecord(e->ev1, e->stream));
+  ENS_CUDA(e, cudaEventSynchronize(e->ev1));
+  ENS_CUDA(e, cudaEventElapsedTime(ms, e->ev0, e->ev1));
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_synchronize(spkgpu_ensemble *e) {
+  if (!e) return SPKGPU_ERR_ARG;
+  ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  EnsCtl c;
+  ENS_CUDA(e, cudaMemcpy(&c, e->d_ctl, sizeof(c), cudaMemcpyDeviceToHost));
+  if (c.err) return ens_fail(e, SPKGPU_ERR_DEVICE, "grid barrier wait gave up");
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_get_stats(spkgpu_ensemble *e, spkgpu_ensemble_stats *out) {
+  if (!e || !out) return SPKGPU_ERR_ARG;
+  int rc = spkgpu_ensemble_synchronize(e);
+  if (rc) return rc;
+  EnsCtl c;
+  ENS_CUDA(e, cudaMemcpy(&c, e->d_ctl, sizeof(c), cudaMemcpyDeviceToHost));
+  out->naccept = (int64_t)c.naccept;
+  out->nattempt = e->nsites * e->nsweeps_done;
+  out->nsweeps = e->nsweeps_done;
+  out->exchange_tries = (int64_t)c.xtries;
+  out->exchange_accepts = (int64_t)c.xaccepts;
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_temperatures(spkgpu_ensemble *e, double *temperature) {
+  if (!e || !temperature) return SPKGPU_ERR_ARG;
+  int rc = spkgpu_ensemble_synchronize(e);
+  if (rc) return rc;
+  std::vector<int32_t> tidx(e->d.nreplica);
+  ENS_CUDA(e, cudaMemcpy(tidx.data(), e->d_tidx, tidx.size() * 4, cudaMemcpyDeviceToHost));
+  for (int r = 0; r < e->d.nreplica; r++) temperature[r] = e->T0[tidx[r]];
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_energies(spkgpu_ensemble *e, int64_t *bonds) {
+  if (!e || !bonds) return SPKGPU_ERR_ARG;
+  int rc = spkgpu_ensemble_synchronize(e);
+  if (rc) return rc;
+  ENS_CUDA(e, cudaMemcpy(bonds, e->d_last_bonds, (size_t)e->d.nreplica * 8, cudaMemcpyDeviceToHost));
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_launch_count(const spkgpu_ensemble *e, int64_t *count) {
+  if (!e || !count) return SPKGPU_ERR_ARG;
+  *count = e->launches;
+  return SPKGPU_OK;
+}
+
+}  // extern "C"

@@ -147,6 +147,7 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
     return SPKGPU_ERR_ARG;
   }
   if (d.rng != SPKGPU_RNG_PHILOX && d.rng != SPKGPU_RNG_STRICT) return SPKGPU_ERR_ARG;
+  if (d.variant != 0 && d.variant != 1) return SPKGPU_ERR_ARG;
   if (d.rng == SPKGPU_RNG_STRICT && d.nsector > 1) return SPKGPU_ERR_ARG;  // src/app_lattice.cpp:155-156
   // colouring needs even extents (Lattice::ncolors, src/lattice.cpp:187-228)
   if (d.nx % 2 || d.ny % 2 || (!spk::is2d(d.lattice) && d.nz % 2)) return SPKGPU_ERR_ARG;
@@ -218,7 +219,7 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
     return fail(SPKGPU_ERR_CUDA);
   }
   h->axes = ax;
-  h->fused_ok = (d.nsector == 1 && d.procs[0] * d.procs[1] * d.procs[2] >= 1 && d.nloop == 1 &&
+  h->fused_ok = (d.variant == 0 && d.nsector == 1 && d.nloop == 1 &&
                  d.rng == SPKGPU_RNG_PHILOX && !d.mask &&
                  spk::fused2d_supported(d.lattice, d.app, sb, d.nx, d.ny));
   if (h->fused_ok) {

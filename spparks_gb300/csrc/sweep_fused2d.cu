@@ -1,10 +1,67 @@
-// Fused whole-sweep tile kernel for 2d lattices (filled in below).
+// Fused sq/4n sweep of a single lattice: one launch per sweep, one CTA per
+// 32x32 tile, both colours of the sweep in shared memory (tile_sweep.cuh),
+// reading one buffer and writing the other.  Used by spkgpu_sweep for sq/4n
+// lattices without sectors, mask or strict RNG whose extents are multiples of
+// 32; every other configuration takes the generic phase kernel.
+
 #include "spk_internal.h"
+#include "tile_sweep.cuh"
 
 namespace spk {
 
-bool fused2d_supported(int, int, int, int, int) { return false; }
+template <int APP, typename S>
+__global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
+  __shared__ S stage[kStage * kStage];
+  __shared__ uint64_t thr[5];
+  if (threadIdx.x < 5) thr[threadIdx.x] = a.acc.thr[threadIdx.x];
+  int tpr = a.nx / kTile;
+  TileJob j;
+  j.src = a.src;
+  j.dst = a.dst;
+  j.L = a.nx;
+  j.Ly = a.ny;
+  j.x0 = (blockIdx.x % tpr) * kTile;
+  j.y0 = (blockIdx.x / tpr) * kTile;
+  j.base = 0;
+  j.seed = a.seed;
+  j.key1 = kStreamSweep;
+  j.sweep = a.sweep;
+  j.nspins = a.nspins;
+  j.zero_t = a.acc.zero_t;
+  j.thr = thr;
+  int changed = tile_sweep_sq4<APP, S>(j, stage);
+  unsigned int w = __reduce_add_sync(0xFFFFFFFFu, (unsigned)changed);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(a.naccept, (unsigned long long)w);
+}
 
-cudaError_t launch_fused2d(int, int, int, const FusedArgs &, cudaStream_t, int) { return cudaErrorNotSupported; }
+bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny) {
+  (void)app;
+  return lattice == SPKGPU_SQ_4N && nx % kTile == 0 && ny % kTile == 0 &&
+         (spin_bytes == 1 || spin_bytes == 2 || spin_bytes == 4);
+}
+
+template <typename S>
+static cudaError_t launch_fused_t(int app, const FusedArgs &a, cudaStream_t s) {
+  unsigned tiles = (unsigned)((a.nx / kTile) * (a.ny / kTile));
+  switch (app) {
+    case SPKGPU_ISING: fused2d_kernel<SPKGPU_ISING, S><<<tiles, kTileThreads, 0, s>>>(a); break;
+    case SPKGPU_POTTS: fused2d_kernel<SPKGPU_POTTS, S><<<tiles, kTileThreads, 0, s>>>(a); break;
+    case SPKGPU_POTTS_NEIGHONLY: fused2d_kernel<SPKGPU_POTTS_NEIGHONLY, S><<<tiles, kTileThreads, 0, s>>>(a); break;
+    case SPKGPU_POTTS_NEIGH: fused2d_kernel<SPKGPU_POTTS_NEIGH, S><<<tiles, kTileThreads, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fused2d(int lattice, int app, int spin_bytes, const FusedArgs &a, cudaStream_t s, int num_sms) {
+  (void)num_sms;
+  if (!fused2d_supported(lattice, app, spin_bytes, a.nx, a.ny)) return cudaErrorNotSupported;
+  switch (spin_bytes) {
+    case 1: return launch_fused_t<int8_t>(app, a, s);
+    case 2: return launch_fused_t<int16_t>(app, a, s);
+    case 4: return launch_fused_t<int32_t>(app, a, s);
+  }
+  return cudaErrorInvalidValue;
+}
 
 }  // namespace spk

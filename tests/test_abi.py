@@ -51,13 +51,14 @@ def test_version_and_invalid_descriptions(lib):
         dict(lattice=sg.SQ_4N, nsector=8),  # 2d with 8 sectors
         dict(rng=sg.RNG_STRICT, nsector=4),  # color/strict with sectors
         dict(nspins=200, spin_bytes=1),
+        dict(variant=2),
     ]
     for b in bad:
         d = sg.Desc()
         d.lattice, d.nx, d.ny, d.nz = sg.SQ_4N, 8, 8, 1
         d.app, d.nspins, d.spin_bytes, d.nsector, d.nloop = sg.POTTS, 5, 0, 1, 1
         d.procs[0] = d.procs[1] = d.procs[2] = 1
-        d.rng, d.mask, d.seed, d.device = 0, 0, 1, 0
+        d.rng, d.mask, d.seed, d.device, d.variant = 0, 0, 1, 0, 0
         for k, v in b.items():
             setattr(d, k, v)
         h = ctypes.c_void_p()
