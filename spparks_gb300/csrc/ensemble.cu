@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kTileThreads) ensemble_kernel(EnsArgs a) {
       j.Ly = L;
       j.x0 = (lt % tpr) * kTile;
       j.y0 = (lt / tpr) * kTile;
-      j.base = a.base[r];
+      j.base = 0;  // replicas differ by Philox stream word; site counter is local
       j.seed = a.seed;
       j.key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
       j.sweep = sweep0 + (uint32_t)s;

@@ -38,7 +38,7 @@ struct TileJob {
   int L;              // replica edge: sites per row and rows (square)
   int Ly;             // rows
   int x0, y0;         // tile origin
-  int64_t base;       // global index of the replica's site 0 (Philox site counter)
+  int64_t base;       // added to the Philox site counter (0: counters are per lattice)
   uint32_t seed, key1, sweep;
   int nspins;
   int zero_t;
