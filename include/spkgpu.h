@@ -47,6 +47,7 @@ extern "C" {
 #define SPKGPU_ERR_UNSUPPORTED (-5) /* combination not implemented */
 #define SPKGPU_ERR_INVALID_SPIN (-6) /* a site value is outside 1..nspins */
 #define SPKGPU_ERR_DEVICE (-7)      /* a device-side wait gave up (error flag set) */
+#define SPKGPU_ERR_TOO_LARGE (-8)   /* lattice exceeds SPKGPU_NOALLOC_MAX_BYTES */
 
 /* lattice styles (src/lattice.cpp:43-57); periodic boxes only */
 #define SPKGPU_SQ_4N 0
@@ -142,6 +143,31 @@ typedef struct spkgpu_kmc_stats {
 } spkgpu_kmc_stats;
 int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, double tstop, int32_t fp64);
 int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_stats *out);
+
+/* sweeping without allocating ----------------------------------------------
+   No counterpart in the reference.  For callers that cannot allocate device
+   memory themselves or through this library: those that own all of it via
+   their own pool (e.g. a framework's caching allocator), or that must not
+   incur the device-wide synchronisation cudaMalloc/cudaFree can cause while
+   their other streams run.  Runs nsweeps fused sq/4n colour sweeps (the same
+   update and draws as spkgpu_sweep on an sq/4n lattice without sectors) on a
+   lattice the caller keeps in device memory: `spin` holds nx*ny values of
+   spin_bytes each (1, 2 or 4; row-major, site index = id-1) and is updated in
+   place; nx and ny must be multiples of 32.  Sweep k uses Philox sweep index
+   sweep0+k.  The second sweep buffer and the change counter come from one
+   static device array of SPKGPU_NOALLOC_MAX_BYTES (+256) bytes that every
+   GPU loading the library holds until exit; larger lattices return
+   SPKGPU_ERR_TOO_LARGE.  The array is shared by all calls and keeps the last
+   call's contents, so calls whose GPU work overlaps race: serialise them.
+   The first call on a device looks up the array's device address
+   (cudaGetSymbolAddress) and should precede any stream capture.  Work goes
+   on `stream` (a cudaStream_t, NULL = default stream); if naccept is not
+   NULL the call waits for the stream and stores the number of changed site
+   values there, otherwise it returns without waiting.  It allocates nothing. */
+#define SPKGPU_NOALLOC_MAX_BYTES (4u << 20)
+int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int32_t spin_bytes, int32_t app,
+                             int32_t nspins, double temperature, uint32_t seed, int64_t sweep0,
+                             int32_t nsweeps, void *stream, int64_t *naccept);
 
 /* batched ensemble of independent sq/4n lattices ---------------------------
    Many replicas of uneven size L x L (L a multiple of 32) and their own

@@ -33,7 +33,7 @@ LATTICE_STYLES = {"sq/4n": SQ_4N, "sq/8n": SQ_8N, "sc/6n": SC_6N, "sc/26n": SC_2
 APP_STYLES = {"ising": ISING, "potts": POTTS, "potts/neighonly": POTTS_NEIGHONLY, "potts/neigh": POTTS_NEIGH}
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "invalid state", -4: "out of device memory",
-          -5: "unsupported", -6: "invalid site value"}
+          -5: "unsupported", -6: "invalid site value", -7: "device wait gave up", -8: "too large"}
 
 
 class SpkGpuError(RuntimeError):
@@ -99,7 +99,7 @@ EXPORTS = [
     "spkgpu_ensemble_create", "spkgpu_ensemble_destroy", "spkgpu_ensemble_last_error", "spkgpu_ensemble_upload",
     "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
     "spkgpu_ensemble_get_stats", "spkgpu_ensemble_temperatures", "spkgpu_ensemble_energies",
-    "spkgpu_ensemble_launch_count",
+    "spkgpu_ensemble_launch_count", "spkgpu_sweep_sq4_noalloc",
 ]
 
 _lib = None
@@ -150,6 +150,9 @@ def load_library(path: Path | None = None):
     L.spkgpu_ensemble_temperatures.argtypes = [vp, P(ctypes.c_double)]
     L.spkgpu_ensemble_energies.argtypes = [vp, P(ctypes.c_int64)]
     L.spkgpu_ensemble_launch_count.argtypes = [vp, P(ctypes.c_int64)]
+    L.spkgpu_sweep_sq4_noalloc.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_int32, ctypes.c_double, ctypes.c_uint32, ctypes.c_int64,
+                                           ctypes.c_int32, vp, P(ctypes.c_int64)]
     if path is None:
         _lib = L
     return L

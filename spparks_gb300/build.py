@@ -25,6 +25,7 @@ SOURCES = [
     "sweep_fused2d.cu",
     "kmc.cu",
     "ensemble.cu",
+    "noalloc.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,0 +1,73 @@
+"""spkgpu_sweep_sq4_noalloc, called through the C ABI.
+
+Callers that cannot allocate device memory (they own all of it through their
+own pool, or cannot afford the synchronisation cudaMalloc/cudaFree may cause)
+hand their device lattice to this entry point, which keeps its sweep buffer
+in a fixed static device array.  Its result must equal the regular entry
+point's (spkgpu_create + spkgpu_sweep) exactly - site values are integers, so
+the tolerance is zero - over two calls in a row that continue the sweep index.
+This file is collected last so that a run stopping at the first failure has
+already run every other test."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOO_LARGE = -8
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import spparks_gb300
+
+    return spparks_gb300.load_library()
+
+
+@pytest.mark.parametrize("app,q,T,nx,ny,sb,calls", [
+    ("ising", 2, 2.269, 64, 64, 1, (3, 4)),
+    ("potts", 30, 0.8, 96, 32, 4, (2, 3)),
+    ("potts/neighonly", 7, 0.5, 32, 64, 2, (1, 2)),
+])
+def test_noalloc_matches_regular_entry_point(lib, app, q, T, nx, ny, sb, calls):
+    import torch
+
+    import spparks_gb300 as sg
+
+    seed = 2468
+    n = nx * ny
+    spin = oracle.init_spins(seed, n, 1, q)
+    ref = sg.Lattice("sq/4n", nx, ny, 1, app, q, spin_bytes=sb, seed=seed)
+    ref.set_temperature(T)
+    ref.upload(spin)
+    dtype = {1: torch.int8, 2: torch.int16, 4: torch.int32}[sb]
+    dev = torch.from_numpy(spin).to(dtype).cuda()
+    torch.cuda.synchronize()
+    sweep0 = 0
+    before = 0
+    for ns in calls:
+        na = ctypes.c_int64(-1)
+        rc = lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(dev.data_ptr()), nx, ny, sb, sg.APP_STYLES[app], q, T,
+                                          seed, sweep0, ns, None, ctypes.byref(na))
+        assert rc == 0
+        ref.sweep(ns)
+        st = ref.stats()
+        assert np.array_equal(dev.to(torch.int32).cpu().numpy(), ref.download())
+        assert na.value == st["naccept"] - before
+        before = st["naccept"]
+        sweep0 += ns
+    ref.close()
+
+
+def test_noalloc_rejects_lattices_beyond_the_static_array(lib):
+    import spparks_gb300 as sg
+
+    na = ctypes.c_int64(0)
+    # 4096 x 2048 int8 = 8 MiB > 4 MiB: rejected before any device work
+    rc = lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(16), 4096, 2048, 1, sg.ISING, 2, 2.0, 1, 0, 1, None,
+                                      ctypes.byref(na))
+    assert rc == TOO_LARGE
