@@ -1,11 +1,667 @@
-// Rejection-free KMC with the tree solver over sectors (filled in below).
+// Rejection-free KMC with the tree solver over sectors: the device form of
+// AppLattice::setup (KMC part, src/app_lattice.cpp:340-377) and
+// AppLattice::iterate_kmc_sector (src/app_lattice.cpp:517-626) driving
+// SolveTree (src/solve_tree.cpp:70-224) and the apps' site_propensity /
+// site_event (src/app_potts.cpp:153-244, src/app_ising.cpp:143-196).
+//
+// Sets ("chains") are the sectors of every processor sub-domain of the
+// `processors` grid; chain c = proc * nsector + (sector-1).  In one sector
+// phase the chains of that sector index on all processors touch disjoint
+// sites, so they run concurrently, one warp each - the reference's own
+// parallel schedule, with the serial 1x1x1 grid as the special case.
+//
+// Per pass and sector phase:
+//   border refresh   kmc_prop_kernel over the border sites of the phase's
+//                    chains (site_propensity -> tree leaf)
+//   tree rebuild     kmc_build_kernel: every internal node = left + right,
+//                    bottom-up, and the count of positive leaves.  This is
+//                    bit-identical to the reference's sequence of
+//                    SolveTree::set calls: the last set() touching a node
+//                    adds the final values of its two children.
+//   event loop       kmc_event_kernel, one warp per chain: pick a leaf with
+//                    find(u0*sum), clock -1/sum*log(u1), stop when the
+//                    sector time reaches dt_kmc (that event discarded), else
+//                    perform site_event (event choice u2*propensity),
+//                    recompute the propensity of the site and its in-chain
+//                    neighbours and re-add their ancestor paths.
+// Philox draws: event k of chain c uses block (c, k): words 0, 1, 2.
+// Propensities are FP64 (exp from a host table, same as the reference's
+// exp) or FP32; tree sums, the root and the clock are FP64 always.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "site_update.cuh"
 #include "spk_internal.h"
 
-void spk_kmc_free(spkgpu_lattice *) {}
+namespace spk {
 
-extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t, double, double, int32_t) {
-  return spk_fail(h, SPKGPU_ERR_UNSUPPORTED, "KMC not built yet");
+struct KmcArgs {
+  void *spin;
+  int nx, ny, nz;
+  int nspins;
+  int zero_t;
+  double pexp[kMaxNeigh + 1];   // exp(-dE/T), FP64
+  float pexpf[kMaxNeigh + 1];   // the same in FP32
+  const int32_t *setof;         // chain of each site
+  const int32_t *i2site;        // index of each site within its chain
+  const int32_t *site2i;        // sites of all chains, chain after chain
+  const int64_t *c_site_off;    // first entry of chain c in site2i
+  const int32_t *c_nloc;        // sites of chain c
+  const int64_t *c_tree_off;    // first node of chain c's tree
+  const int32_t *c_leaf0;       // leaf offset (nround-1) of chain c's tree
+  const int32_t *c_ntotal;      // nodes of chain c's tree (2*nround-1)
+  int32_t *c_nactive;           // positive leaves of chain c
+  unsigned long long *c_events; // Philox event counter of chain c
+  double *trees;
+  unsigned long long *pmax_bits;  // max over chains of sum/num_active (as bits)
+  unsigned long long *naccept;
+  int nsector;
+  int nprocs;
+  uint32_t seed;
+  double dt_kmc;
+  int fp64;
+  int smem_trees;               // 1: the event kernel copies trees to shared memory
+};
+
+template <int LAT>
+__device__ __forceinline__ void site_coords(int64_t i, int nx, int ny, int &x, int &y, int &z) {
+  x = (int)(i % nx);
+  int64_t r = i / nx;
+  y = (int)(r % ny);
+  z = (int)(r / ny);
 }
-extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *, double, spkgpu_kmc_stats *) {
-  return spk_fail(h, SPKGPU_ERR_UNSUPPORTED, "KMC not built yet");
+
+template <int LAT>
+__device__ __forceinline__ int64_t neighbor_of(int x, int y, int z, int j, int nx, int ny, int nz) {
+  int dx, dy, dz;
+  Stencil<LAT>::offset(j, dx, dy, dz);
+  int xn = x + dx, yn = y + dy, zn = z + dz;
+  xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
+  yn = yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn);
+  if (Stencil<LAT>::k3d) zn = zn < 0 ? zn + nz : (zn >= nz ? zn - nz : zn);
+  else zn = 0;
+  return (int64_t)xn + (int64_t)nx * ((int64_t)yn + (int64_t)ny * zn);
+}
+
+template <typename S, int LAT>
+__device__ __forceinline__ void load_neighbors(const S *spin, int64_t i, int nx, int ny, int nz,
+                                               int (&nb)[Stencil<LAT>::NN]) {
+  int x, y, z;
+  site_coords<LAT>(i, nx, ny, x, y, z);
+#pragma unroll
+  for (int j = 0; j < Stencil<LAT>::NN; j++) nb[j] = (int)spin[neighbor_of<LAT>(x, y, z, j, nx, ny, nz)];
+}
+
+// site_propensity: Ising flip (src/app_ising.cpp:143-163) or the sum over
+// distinct unlike neighbour values (src/app_potts.cpp:153-189), summed in the
+// reference's order
+template <typename S, int LAT, int APP>
+__device__ double site_propensity(const KmcArgs &a, const S *spin, int64_t i) {
+  constexpr int NN = Stencil<LAT>::NN;
+  int nb[NN];
+  load_neighbors<S, LAT>(spin, i, a.nx, a.ny, a.nz, nb);
+  int own = (int)spin[i];
+  int e0 = count_unlike<NN>(own, nb);
+  if (APP == SPKGPU_ISING) {
+    int e1 = count_unlike<NN>(own == 1 ? 2 : 1, nb);
+    if (e1 <= e0) return 1.0;
+    if (a.zero_t) return 0.0;
+    return a.fp64 ? a.pexp[e1 - e0] : (double)a.pexpf[e1 - e0];
+  }
+  uint32_t first = first_appearance<NN>(own, nb);
+  if (a.fp64) {
+    double prob = 0.0;
+#pragma unroll
+    for (int j = 0; j < NN; j++) {
+      if (!((first >> j) & 1u)) continue;
+      int e1 = count_unlike<NN>(nb[j], nb);
+      if (e1 <= e0) prob += 1.0;
+      else if (!a.zero_t) prob += a.pexp[e1 - e0];
+    }
+    return prob;
+  }
+  float prob = 0.0f;
+#pragma unroll
+  for (int j = 0; j < NN; j++) {
+    if (!((first >> j) & 1u)) continue;
+    int e1 = count_unlike<NN>(nb[j], nb);
+    if (e1 <= e0) prob += 1.0f;
+    else if (!a.zero_t) prob += a.pexpf[e1 - e0];
+  }
+  return (double)prob;
+}
+
+// propensities of listed sites (or all sites) into their tree leaves
+template <typename S, int LAT, int APP>
+__global__ void kmc_prop_kernel(KmcArgs a, const int32_t *list, int64_t nlist) {
+  const S *spin = (const S *)a.spin;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nlist; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = list ? (int64_t)list[t] : t;
+    int c = a.setof[i];
+    a.trees[a.c_tree_off[c] + a.c_leaf0[c] + a.i2site[i]] = site_propensity<S, LAT, APP>(a, spin, i);
+  }
+}
+
+// bottom-up rebuild of the trees of chains (proc*nsector + iset), one CTA
+// per chain (iset < 0: every chain), and the count of positive leaves
+__global__ void kmc_build_kernel(KmcArgs a, int iset) {
+  int c = (iset < 0) ? blockIdx.x : blockIdx.x * a.nsector + iset;
+  double *T = a.trees + a.c_tree_off[c];
+  int leaf0 = a.c_leaf0[c];
+  int ntotal = a.c_ntotal[c];
+  // levels: internal nodes of depth d are [2^d - 1, 2^(d+1) - 1)
+  int depth = 0;
+  while ((1 << depth) - 1 < leaf0) depth++;
+  for (int d = depth - 1; d >= 0; d--) {
+    int lo = (1 << d) - 1, hi = (1 << (d + 1)) - 1;
+    for (int p = lo + threadIdx.x; p < hi; p += blockDim.x) T[p] = T[2 * p + 1] + T[2 * p + 2];
+    __syncthreads();
+  }
+  int cnt = 0;
+  for (int p = leaf0 + threadIdx.x; p < ntotal; p += blockDim.x) cnt += T[p] > 0.0;
+  cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
+  __shared__ int red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) tot += red[w];
+    a.c_nactive[c] = tot;
+  }
+}
+
+// SolveTree::find (src/solve_tree.cpp:207-224)
+__device__ __forceinline__ int tree_find(const double *T, int leaf0, double value) {
+  int i = 0;
+  while (i < leaf0) {
+    int left = 2 * i + 1;
+    double tl = T[left];
+    if (value <= tl) i = left;
+    else {
+      value -= tl;
+      i = left + 1;
+    }
+  }
+  return i - leaf0;
+}
+
+// one warp per chain of sector iset: the event loop of iterate_kmc_sector
+template <typename S, int LAT, int APP>
+__global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
+  constexpr int NN = Stencil<LAT>::NN;
+  extern __shared__ double smem_tree[];
+  const int lane = threadIdx.x;
+  const int c = blockIdx.x * a.nsector + iset;
+  S *spin = (S *)a.spin;
+  double *G = a.trees + a.c_tree_off[c];
+  const int leaf0 = a.c_leaf0[c];
+  const int ntotal = a.c_ntotal[c];
+  double *T = G;
+  if (a.smem_trees) {
+    for (int p = lane; p < ntotal; p += 32) smem_tree[p] = G[p];
+    T = smem_tree;
+    __syncwarp();
+  }
+  const int32_t *site2i = a.site2i + a.c_site_off[c];
+  int nactive = a.c_nactive[c];
+  unsigned long long k = a.c_events[c];
+  double sum = T[0];
+  // pmax = maximum sector propensity per active site (src/app_lattice.cpp:563-573)
+  if (lane == 0 && nactive > 0) {
+    double ptmp = sum / nactive;
+    atomicMax(a.pmax_bits, (unsigned long long)__double_as_longlong(ptmp));
+  }
+  double timesector = 0.0;
+  unsigned int done_events = 0;
+  while (sum != 0.0) {
+    U4 w = kmc_block(a.seed, (uint32_t)c, k);
+    k++;
+    int m = 0;
+    if (lane == 0) m = tree_find(T, leaf0, word_to_uniform(w.x) * sum);
+    m = __shfl_sync(0xFFFFFFFFu, m, 0);
+    double dt = -1.0 / sum * log(word_to_uniform(w.y));
+    timesector += dt;
+    if (timesector >= a.dt_kmc) break;
+    int64_t i = site2i[m];
+    int x, y, z;
+    site_coords<LAT>(i, a.nx, a.ny, x, y, z);
+    // site_event
+    if (lane == 0) {
+      int own = (int)spin[i];
+      if (APP == SPKGPU_ISING) {
+        spin[i] = (S)(own == 1 ? 2 : 1);
+      } else {
+        int nb[NN];
+        load_neighbors<S, LAT>(spin, i, a.nx, a.ny, a.nz, nb);
+        double threshhold = word_to_uniform(w.z) * T[leaf0 + m];
+        int e0 = count_unlike<NN>(own, nb);
+        uint32_t first = first_appearance<NN>(own, nb);
+        int value = own;
+        if (a.fp64) {
+          double prob = 0.0;
+          for (int j = 0; j < NN; j++) {
+            if (!((first >> j) & 1u)) continue;
+            value = nb[j];
+            int e1 = count_unlike<NN>(value, nb);
+            if (e1 <= e0) prob += 1.0;
+            else if (!a.zero_t) prob += a.pexp[e1 - e0];
+            if (prob >= threshhold) break;
+          }
+        } else {
+          float prob = 0.0f;
+          for (int j = 0; j < NN; j++) {
+            if (!((first >> j) & 1u)) continue;
+            value = nb[j];
+            int e1 = count_unlike<NN>(value, nb);
+            if (e1 <= e0) prob += 1.0f;
+            else if (!a.zero_t) prob += a.pexpf[e1 - e0];
+            if ((double)prob >= threshhold) break;
+          }
+        }
+        spin[i] = (S)value;
+      }
+    }
+    __syncwarp();
+    // propensity of the site (entry 0) and its in-chain neighbours (1..NN)
+    int64_t s = -1;
+    if (lane == 0) s = i;
+    else if (lane <= NN) {
+      int64_t nbi = neighbor_of<LAT>(x, y, z, lane - 1, a.nx, a.ny, a.nz);
+      if (a.setof[nbi] == c) s = nbi;
+    }
+    double p = 0.0;
+    int leaf = -1;
+    if (s >= 0) {
+      p = site_propensity<S, LAT, APP>(a, spin, s);
+      leaf = a.i2site[s];
+    }
+    // leaves in the reference's order (self, then neighbours in order);
+    // num_active as SolveTree::set counts it
+    for (int j = 0; j <= NN; j++) {
+      int lj = __shfl_sync(0xFFFFFFFFu, leaf, j);
+      double pj = __shfl_sync(0xFFFFFFFFu, p, j);
+      if (lj < 0) continue;
+      if (lane == 0) {
+        double old = T[leaf0 + lj];
+        nactive += (pj > 0.0) - (old > 0.0);
+        T[leaf0 + lj] = pj;
+      }
+      __syncwarp();
+    }
+    // re-add the ancestor paths, level by level (lanes that share a node
+    // write the same value)
+    int node = leaf >= 0 ? leaf0 + leaf : -1;
+    while (__any_sync(0xFFFFFFFFu, node > 0)) {
+      if (node > 0) {
+        int parent = (node - 1) >> 1;
+        T[parent] = T[2 * parent + 1] + T[2 * parent + 2];
+        node = parent;
+      }
+      __syncwarp();
+    }
+    sum = T[0];
+    done_events++;
+  }
+  if (lane == 0) {
+    a.c_events[c] = k;
+    a.c_nactive[c] = nactive;
+    if (done_events) atomicAdd(a.naccept, (unsigned long long)done_events);
+  }
+  if (a.smem_trees) {
+    __syncwarp();
+    for (int p = lane; p < ntotal; p += 32) G[p] = T[p];
+  }
+}
+
+}  // namespace spk
+
+using namespace spk;
+
+struct KmcState {
+  int ready = 0;
+  int adapt = 1;
+  double nstop = 1.0, tstop = 0.0;
+  int fp64 = 1;
+  int nchains = 0;
+  int64_t nsites = 0;
+  double dt_kmc = 0.0;
+  int64_t naccept_base = 0;
+  int64_t npass = 0;
+  int max_ntotal = 0;
+  std::vector<int64_t> border_off;  // per sector: offset into border list (nsector+1)
+  int32_t *d_setof = nullptr, *d_i2site = nullptr, *d_site2i = nullptr, *d_border = nullptr;
+  int64_t *d_site_off = nullptr, *d_tree_off = nullptr;
+  int32_t *d_nloc = nullptr, *d_leaf0 = nullptr, *d_ntotal = nullptr, *d_nactive = nullptr;
+  unsigned long long *d_events = nullptr;
+  double *d_trees = nullptr;
+  unsigned long long *d_scalars = nullptr;  // [0] pmax bits, [1] naccept
+  std::vector<int32_t> h_nactive;
+};
+
+void spk_kmc_free(spkgpu_lattice *h) {
+  if (!h || !h->kmc) return;
+  KmcState *k = h->kmc;
+  cudaFree(k->d_setof);
+  cudaFree(k->d_i2site);
+  cudaFree(k->d_site2i);
+  cudaFree(k->d_border);
+  cudaFree(k->d_site_off);
+  cudaFree(k->d_tree_off);
+  cudaFree(k->d_nloc);
+  cudaFree(k->d_leaf0);
+  cudaFree(k->d_ntotal);
+  cudaFree(k->d_nactive);
+  cudaFree(k->d_events);
+  cudaFree(k->d_trees);
+  cudaFree(k->d_scalars);
+  delete k;
+  h->kmc = nullptr;
+}
+
+#define KMC_CUDA(h, call)                                   \
+  do {                                                      \
+    cudaError_t e__ = (call);                               \
+    if (e__ != cudaSuccess) return spk_cuda_fail(h, e__, #call); \
+  } while (0)
+
+static KmcArgs kmc_args(spkgpu_lattice *h) {
+  KmcState *k = h->kmc;
+  KmcArgs a;
+  memset(&a, 0, sizeof(a));
+  a.spin = h->d_spin;
+  a.nx = h->d.nx;
+  a.ny = h->d.ny;
+  a.nz = h->d.nz;
+  a.nspins = h->d.nspins;
+  a.zero_t = h->acc.zero_t;
+  for (int d = 0; d <= kMaxNeigh; d++) {
+    a.pexp[d] = h->acc.pexp[d];
+    a.pexpf[d] = (float)h->acc.pexp[d];
+  }
+  a.setof = k->d_setof;
+  a.i2site = k->d_i2site;
+  a.site2i = k->d_site2i;
+  a.c_site_off = k->d_site_off;
+  a.c_nloc = k->d_nloc;
+  a.c_tree_off = k->d_tree_off;
+  a.c_leaf0 = k->d_leaf0;
+  a.c_ntotal = k->d_ntotal;
+  a.c_nactive = k->d_nactive;
+  a.c_events = k->d_events;
+  a.trees = k->d_trees;
+  a.pmax_bits = k->d_scalars;
+  a.naccept = k->d_scalars + 1;
+  a.nsector = h->d.nsector;
+  a.nprocs = k->nchains / h->d.nsector;
+  a.seed = h->d.seed;
+  a.dt_kmc = k->dt_kmc;
+  a.fp64 = k->fp64;
+  a.smem_trees = ((size_t)k->max_ntotal * 8 <= 48 * 1024) ? 1 : 0;
+  return a;
+}
+
+template <typename S, int LAT>
+static cudaError_t launch_prop_t(int app, const KmcArgs &a, const int32_t *list, int64_t n, cudaStream_t s, int sms) {
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = std::min<int64_t>((n + 127) / 128, (int64_t)sms * 16);
+  if (app == SPKGPU_ISING) kmc_prop_kernel<S, LAT, SPKGPU_ISING><<<(unsigned)blocks, 128, 0, s>>>(a, list, n);
+  else kmc_prop_kernel<S, LAT, SPKGPU_POTTS><<<(unsigned)blocks, 128, 0, s>>>(a, list, n);
+  return cudaGetLastError();
+}
+
+template <typename S, int LAT>
+static cudaError_t launch_events_t(int app, const KmcArgs &a, int iset, int nprocs, size_t smem, cudaStream_t s) {
+  if (app == SPKGPU_ISING) {
+    auto f = kmc_event_kernel<S, LAT, SPKGPU_ISING>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    f<<<nprocs, 32, smem, s>>>(a, iset);
+  } else {
+    auto f = kmc_event_kernel<S, LAT, SPKGPU_POTTS>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    f<<<nprocs, 32, smem, s>>>(a, iset);
+  }
+  return cudaGetLastError();
+}
+
+template <typename S>
+static cudaError_t dispatch_lat(int lattice, int app, int what, const KmcArgs &a, const int32_t *list, int64_t n,
+                                int iset, int nprocs, size_t smem, cudaStream_t s, int sms) {
+#define SPK_KMC_CASE(LATV)                                                                   \
+  case LATV:                                                                                 \
+    return what == 0 ? launch_prop_t<S, LATV>(app, a, list, n, s, sms)                       \
+                     : launch_events_t<S, LATV>(app, a, iset, nprocs, smem, s);
+  switch (lattice) {
+    SPK_KMC_CASE(SPKGPU_SQ_4N)
+    SPK_KMC_CASE(SPKGPU_SQ_8N)
+    SPK_KMC_CASE(SPKGPU_SC_6N)
+    SPK_KMC_CASE(SPKGPU_SC_26N)
+  }
+#undef SPK_KMC_CASE
+  return cudaErrorInvalidValue;
+}
+
+static cudaError_t kmc_launch(spkgpu_lattice *h, int what, const KmcArgs &a, const int32_t *list, int64_t n,
+                              int iset) {
+  KmcState *k = h->kmc;
+  int nprocs = k->nchains / h->d.nsector;
+  size_t smem = a.smem_trees ? (size_t)k->max_ntotal * 8 : 0;
+  h->launches++;
+  switch (h->spin_bytes) {
+    case 1: return dispatch_lat<int8_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, h->stream, h->num_sms);
+    case 2: return dispatch_lat<int16_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, h->stream, h->num_sms);
+    case 4: return dispatch_lat<int32_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, h->stream, h->num_sms);
+  }
+  return cudaErrorInvalidValue;
+}
+
+extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, double tstop, int32_t fp64) {
+  if (!h) return SPKGPU_ERR_ARG;
+  const spkgpu_desc &d = h->d;
+  if (d.nsector < 2) return spk_fail(h, SPKGPU_ERR_UNSUPPORTED, "KMC on the GPU needs sectors (sector yes|2|4|8)");
+  if (d.rng != SPKGPU_RNG_PHILOX) return spk_fail(h, SPKGPU_ERR_ARG, "KMC uses Philox draws");
+  if (adapt && !(nstop > 0.0)) return spk_fail(h, SPKGPU_ERR_ARG, "nstop must be > 0");
+  if (!adapt && !(tstop > 0.0)) return spk_fail(h, SPKGPU_ERR_ARG, "tstop must be > 0");
+  if (h->n >= (1LL << 31)) return spk_fail(h, SPKGPU_ERR_UNSUPPORTED, "KMC lattices are limited to 2^31 sites");
+  spk_kmc_free(h);
+  KmcState *k = new (std::nothrow) KmcState();
+  if (!k) return SPKGPU_ERR_NOMEM;
+  h->kmc = k;
+  k->adapt = adapt ? 1 : 0;
+  k->nstop = nstop;
+  k->tstop = tstop;
+  k->fp64 = fp64 ? 1 : 0;
+  // chain membership from the handle's processor and sector-half tables
+  std::vector<int32_t> blob_proc[3], blob_half[3];
+  int dims[3] = {d.nx, d.ny, d.nz};
+  for (int ax = 0; ax < 3; ax++) {
+    blob_proc[ax].resize(dims[ax]);
+    blob_half[ax].resize(dims[ax]);
+    KMC_CUDA(h, cudaMemcpy(blob_proc[ax].data(), h->d_axis + h->proc_off[ax], dims[ax] * 4, cudaMemcpyDeviceToHost));
+    KMC_CUDA(h, cudaMemcpy(blob_half[ax].data(), h->d_axis + h->half_off[ax], dims[ax] * 4, cudaMemcpyDeviceToHost));
+  }
+  int nsec = d.nsector;
+  int nprocs = d.procs[0] * d.procs[1] * d.procs[2];
+  k->nchains = nprocs * nsec;
+  int64_t n = h->n;
+  k->nsites = n;
+  std::vector<int32_t> setof(n), i2site(n), nloc(k->nchains, 0);
+  for (int64_t i = 0; i < n; i++) {
+    int x = (int)(i % d.nx);
+    int64_t r = i / d.nx;
+    int y = (int)(r % d.ny);
+    int z = (int)(r / d.ny);
+    int proc = blob_proc[0][x] + d.procs[0] * (blob_proc[1][y] + d.procs[1] * blob_proc[2][z]);
+    int iw = blob_half[0][x], jw = blob_half[1][y], kw = blob_half[2][z];
+    int msector = (nsec == 2) ? iw : (nsec == 4 ? 2 * jw + iw : 4 * kw + 2 * jw + iw);
+    int c = proc * nsec + msector;
+    setof[i] = c;
+    i2site[i] = nloc[c]++;
+  }
+  std::vector<int64_t> site_off(k->nchains + 1, 0), tree_off(k->nchains + 1, 0);
+  std::vector<int32_t> leaf0(k->nchains), ntotal(k->nchains);
+  for (int c = 0; c < k->nchains; c++) {
+    site_off[c + 1] = site_off[c] + nloc[c];
+    int64_t nround = 1;
+    while (nround < nloc[c]) nround *= 2;
+    leaf0[c] = (int32_t)(nround - 1);
+    ntotal[c] = (int32_t)(2 * nround - 1);
+    tree_off[c + 1] = tree_off[c] + ntotal[c];
+    k->max_ntotal = std::max(k->max_ntotal, ntotal[c]);
+  }
+  std::vector<int32_t> site2i(n);
+  for (int64_t i = 0; i < n; i++) site2i[site_off[setof[i]] + i2site[i]] = (int32_t)i;
+  // border sites (a neighbour in another chain), grouped by sector index in
+  // the order chains of that sector appear (find_border_sites,
+  // src/app_lattice.cpp:1094-1149)
+  int nn = h->maxneigh;
+  std::vector<std::vector<int32_t>> border_by_sec(nsec);
+  for (int c = 0; c < k->nchains; c++) {
+    int sec = c % nsec;
+    for (int64_t m = site_off[c]; m < site_off[c + 1]; m++) {
+      int64_t i = site2i[m];
+      int x = (int)(i % d.nx);
+      int64_t r = i / d.nx;
+      int y = (int)(r % d.ny);
+      int z = (int)(r / d.ny);
+      bool border = false;
+      for (int j = 0; j < nn && !border; j++) {
+        int dx = 0, dy = 0, dz = 0;
+        switch (d.lattice) {
+          case SPKGPU_SQ_4N: Stencil<SPKGPU_SQ_4N>::offset(j, dx, dy, dz); break;
+          case SPKGPU_SQ_8N: Stencil<SPKGPU_SQ_8N>::offset(j, dx, dy, dz); break;
+          case SPKGPU_SC_6N: Stencil<SPKGPU_SC_6N>::offset(j, dx, dy, dz); break;
+          default: Stencil<SPKGPU_SC_26N>::offset(j, dx, dy, dz); break;
+        }
+        int xn = (x + dx + d.nx) % d.nx, yn = (y + dy + d.ny) % d.ny, zn = (z + dz + d.nz) % d.nz;
+        int64_t nbi = xn + (int64_t)d.nx * (yn + (int64_t)d.ny * zn);
+        if (setof[nbi] != c) border = true;
+      }
+      if (border) border_by_sec[sec].push_back((int32_t)i);
+    }
+  }
+  std::vector<int32_t> border;
+  k->border_off.assign(nsec + 1, 0);
+  for (int s = 0; s < nsec; s++) {
+    border.insert(border.end(), border_by_sec[s].begin(), border_by_sec[s].end());
+    k->border_off[s + 1] = (int64_t)border.size();
+  }
+  auto dm = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes ? bytes : 16) == cudaSuccess; };
+  if (!dm((void **)&k->d_setof, n * 4) || !dm((void **)&k->d_i2site, n * 4) || !dm((void **)&k->d_site2i, n * 4) ||
+      !dm((void **)&k->d_border, border.size() * 4) || !dm((void **)&k->d_site_off, (k->nchains + 1) * 8) ||
+      !dm((void **)&k->d_tree_off, (k->nchains + 1) * 8) || !dm((void **)&k->d_nloc, k->nchains * 4) ||
+      !dm((void **)&k->d_leaf0, k->nchains * 4) || !dm((void **)&k->d_ntotal, k->nchains * 4) ||
+      !dm((void **)&k->d_nactive, k->nchains * 4) || !dm((void **)&k->d_events, k->nchains * 8) ||
+      !dm((void **)&k->d_trees, tree_off[k->nchains] * 8) || !dm((void **)&k->d_scalars, 4 * 8)) {
+    spk_kmc_free(h);
+    return spk_fail(h, SPKGPU_ERR_NOMEM, "KMC allocation failed");
+  }
+  KMC_CUDA(h, cudaMemcpy(k->d_setof, setof.data(), n * 4, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_i2site, i2site.data(), n * 4, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_site2i, site2i.data(), n * 4, cudaMemcpyHostToDevice));
+  if (!border.empty()) KMC_CUDA(h, cudaMemcpy(k->d_border, border.data(), border.size() * 4, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_site_off, site_off.data(), (k->nchains + 1) * 8, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_tree_off, tree_off.data(), (k->nchains + 1) * 8, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_nloc, nloc.data(), k->nchains * 4, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_leaf0, leaf0.data(), k->nchains * 4, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_ntotal, ntotal.data(), k->nchains * 4, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemset(k->d_events, 0, k->nchains * 8));
+  KMC_CUDA(h, cudaMemset(k->d_trees, 0, tree_off[k->nchains] * 8));
+  KMC_CUDA(h, cudaMemset(k->d_scalars, 0, 4 * 8));
+  k->ready = 1;
+  return SPKGPU_OK;
+}
+
+// pmax over all chains of sum/num_active after a full rebuild
+static int kmc_pmax(spkgpu_lattice *h, double *pmax) {
+  unsigned long long bits = 0;
+  KMC_CUDA(h, cudaMemcpyAsync(&bits, h->kmc->d_scalars, 8, cudaMemcpyDeviceToHost, h->stream));
+  KMC_CUDA(h, cudaStreamSynchronize(h->stream));
+  double v;
+  memcpy(&v, &bits, 8);
+  *pmax = v;
+  return SPKGPU_OK;
+}
+
+extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime, spkgpu_kmc_stats *out) {
+  if (!h || !ptime) return SPKGPU_ERR_ARG;
+  KmcState *k = h->kmc;
+  if (!k || !k->ready) return spk_fail(h, SPKGPU_ERR_STATE, "spkgpu_kmc_setup has not been called");
+  if (!h->have_temperature) return spk_fail(h, SPKGPU_ERR_STATE, "temperature has not been set");
+  const int nsec = h->d.nsector;
+  double time = *ptime;
+  KmcArgs a = kmc_args(h);
+  // setup(): every propensity, every tree (src/app_lattice.cpp:340-347)
+  KMC_CUDA(h, kmc_launch(h, 0, a, nullptr, h->n, 0));
+  kmc_build_kernel<<<k->nchains, 256, 0, h->stream>>>(a, -1);
+  h->launches++;
+  KMC_CUDA(h, cudaGetLastError());
+  if (k->tstop > 0.0 && !k->adapt) k->dt_kmc = k->tstop;
+  if (k->adapt) {
+    // max over sets of sum/num_active (src/app_lattice.cpp:356-371)
+    std::vector<int32_t> nact(k->nchains);
+    std::vector<int64_t> toff(k->nchains + 1);
+    KMC_CUDA(h, cudaMemcpyAsync(nact.data(), k->d_nactive, k->nchains * 4, cudaMemcpyDeviceToHost, h->stream));
+    KMC_CUDA(h, cudaMemcpyAsync(toff.data(), k->d_tree_off, (k->nchains + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+    KMC_CUDA(h, cudaStreamSynchronize(h->stream));
+    double pmax = 0.0;
+    for (int c = 0; c < k->nchains; c++) {
+      if (nact[c] <= 0) continue;
+      double root = 0.0;
+      KMC_CUDA(h, cudaMemcpy(&root, k->d_trees + toff[c], 8, cudaMemcpyDeviceToHost));
+      pmax = std::max(pmax, root / nact[c]);
+    }
+    k->dt_kmc = (pmax > 0.0) ? k->nstop / pmax : stoptime - time;
+  }
+  k->dt_kmc = std::min(k->dt_kmc, stoptime - time);
+  if (stoptime > time) {
+    bool alldone = false;
+    while (!alldone) {
+      KMC_CUDA(h, cudaMemsetAsync(k->d_scalars, 0, 8, h->stream));
+      a.dt_kmc = k->dt_kmc;
+      for (int iset = 0; iset < nsec; iset++) {
+        int64_t b0 = k->border_off[iset], b1 = k->border_off[iset + 1];
+        KMC_CUDA(h, kmc_launch(h, 0, a, k->d_border + b0, b1 - b0, iset));
+        kmc_build_kernel<<<k->nchains / nsec, 256, 0, h->stream>>>(a, iset);
+        h->launches++;
+        KMC_CUDA(h, cudaGetLastError());
+        KMC_CUDA(h, kmc_launch(h, 1, a, nullptr, 0, iset));
+      }
+      k->npass++;
+      time += k->dt_kmc;
+      if (time >= stoptime) alldone = true;
+      if (k->adapt) {
+        double pmax = 0.0;
+        int rc = kmc_pmax(h, &pmax);
+        if (rc) return rc;
+        k->dt_kmc = (pmax > 0.0) ? k->nstop / pmax : stoptime - time;
+        k->dt_kmc = std::min(k->dt_kmc, stoptime - time);
+      }
+    }
+  }
+  *ptime = time;
+  if (out) {
+    unsigned long long na = 0;
+    KMC_CUDA(h, cudaMemcpyAsync(&na, k->d_scalars + 1, 8, cudaMemcpyDeviceToHost, h->stream));
+    KMC_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::vector<int64_t> toff(k->nchains + 1);
+    KMC_CUDA(h, cudaMemcpy(toff.data(), k->d_tree_off, (k->nchains + 1) * 8, cudaMemcpyDeviceToHost));
+    double total = 0.0;
+    for (int c = 0; c < k->nchains; c++) {
+      double root = 0.0;
+      KMC_CUDA(h, cudaMemcpy(&root, k->d_trees + toff[c], 8, cudaMemcpyDeviceToHost));
+      total += root;
+    }
+    out->time = time;
+    out->naccept = (int64_t)na;
+    out->npass = k->npass;
+    out->dt_kmc = k->dt_kmc;
+    out->total_propensity = total;
+  }
+  return SPKGPU_OK;
 }

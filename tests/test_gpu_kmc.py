@@ -1,0 +1,90 @@
+"""GPU parity of rejection-free KMC with the tree solver over sectors
+(spkgpu_kmc_setup / spkgpu_kmc_run): FP64 propensities must reproduce the
+reference (fixtures from the reference with the Philox shim) and the oracle
+restatement exactly - lattice, event count, passes and clock; FP32
+propensities must keep the total propensity within 1e-6 relative of FP64."""
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sg():
+    import spparks_gb300
+
+    spparks_gb300.load_library()
+    return spparks_gb300
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_kmc_matches_reference_fixtures(sg, ref_fixtures, k):
+    fx = ref_fixtures["kmc"][k]
+    c = fx["case"]
+    nsec = 4 if c["lattice"].startswith("sq") else 8
+    lat = sg.Lattice(c["lattice"], c["nx"], c["ny"], c["nz"], c["app"], c["nspins"], nsector=nsec, seed=c["seed"])
+    lat.set_temperature(c["temperature"])
+    lat.upload(np.array(fx["snaps"]["init"]["spins"], dtype=np.int32))
+    lat.kmc_setup(adapt=True, nstop=1.0, fp64=True)
+    t = 0.0
+    npass = 0
+    for r, dt in enumerate(c["runs"]):
+        st = lat.kmc_run(t, t + dt)
+        t = st["time"]
+        assert lat.download().tolist() == fx["snaps"][f"run{r}"]["spins"]
+    ref = fx["sweeps"]
+    assert st["npass"] == len(ref)
+    assert st["naccept"] == ref[-1][1]
+    assert t == pytest.approx(ref[-1][4], rel=1e-12)
+
+
+KMC_CASES = [
+    dict(lattice="sq/8n", nx=32, ny=32, nz=1, app="potts", nspins=10, T=1.0, procs=(2, 2, 1), nsector=4, run=2.0),
+    dict(lattice="sq/4n", nx=24, ny=16, nz=1, app="ising", nspins=2, T=2.0, procs=(3, 2, 1), nsector=4, run=1.5),
+    dict(lattice="sc/26n", nx=12, ny=12, nz=8, app="potts", nspins=20, T=0.8, procs=(2, 1, 1), nsector=8, run=0.4),
+    dict(lattice="sc/6n", nx=12, ny=8, nz=8, app="potts/neighonly", nspins=6, T=0.7, procs=(1, 1, 1), nsector=2,
+         run=1.0),
+]
+
+
+@pytest.mark.parametrize("c", KMC_CASES, ids=lambda c: f"{c['app']}-{c['lattice']}-{c['procs']}")
+def test_kmc_processor_grid_matches_oracle(sg, c):
+    seed = 1357
+    n = c["nx"] * c["ny"] * c["nz"]
+    spin = oracle.init_spins(seed, n, 1, c["nspins"])
+    cfg = oracle.make_cfg(c["lattice"], c["nx"], c["ny"], c["nz"], c["app"], c["nspins"], c["T"], c["nsector"],
+                          seed=seed, procs=c["procs"])
+    km = oracle.Kmc(cfg)
+    ref = spin.copy()
+    npass, _, times = km.run(ref, c["run"])
+    lat = sg.Lattice(c["lattice"], c["nx"], c["ny"], c["nz"], c["app"], c["nspins"], nsector=c["nsector"],
+                     procs=c["procs"], seed=seed)
+    lat.set_temperature(c["T"])
+    lat.upload(spin)
+    lat.kmc_setup(fp64=True)
+    st = lat.kmc_run(0.0, c["run"])
+    assert lat.download().tolist() == ref.tolist()
+    assert st["naccept"] == km.naccept
+    assert st["npass"] == npass
+    assert st["time"] == pytest.approx(km.time, rel=1e-12)
+    assert st["total_propensity"] == pytest.approx(km.total_propensity(), rel=1e-12)
+
+
+def test_kmc_fp32_propensity_error(sg):
+    """FP32 propensities, FP64 tree: relative error of the total propensity
+    against the FP64 path on the same lattice state."""
+    seed = 24
+    nx = ny = 64
+    spin = oracle.init_spins(seed, nx * ny, 1, 50)
+    tot = {}
+    for fp64 in (True, False):
+        lat = sg.Lattice("sq/8n", nx, ny, 1, "potts", 50, nsector=4, procs=(4, 4, 1), seed=seed)
+        lat.set_temperature(1.0)
+        lat.upload(spin)
+        lat.kmc_setup(fp64=fp64)
+        st = lat.kmc_run(0.0, 0.0)
+        tot[fp64] = st["total_propensity"]
+    assert abs(tot[False] - tot[True]) / tot[True] < 1e-6
