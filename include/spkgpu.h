@@ -71,8 +71,10 @@ typedef struct spkgpu_desc {
   int32_t nx, ny, nz;   /* sites per axis; nz = 1 for 2d styles */
   int32_t app;          /* SPKGPU_ISING ... */
   int32_t nspins;       /* Q (2 for Ising); must be < 2^21 */
-  int32_t spin_bytes;   /* device storage per site: 1, 2, 4, or 0 = smallest
-                           that holds nspins */
+  int32_t spin_bytes;   /* device storage per site: 1, 2, 4, 0 = smallest
+                           that holds nspins, or -1 = bit-packed, 64 sites per
+                           uint64 (Ising on sc/6n, nx a multiple of 64, no
+                           sectors, mask or strict RNG) */
   int32_t nsector;      /* 1 = no sectors, else 2, 4, 8 (`sector`) */
   int32_t nloop;        /* passes over each set per sweep (`sector nstop`) */
   int32_t procs[3];     /* processor grid (`processors`), 1 1 1 = serial */
@@ -102,6 +104,11 @@ int spkgpu_set_temperature(spkgpu_lattice *h, double temperature);
 /* site values in App::iarray[0] order (site index = id - 1) */
 int spkgpu_upload_spins(spkgpu_lattice *h, const int32_t *spin, int64_t n);
 int spkgpu_download_spins(spkgpu_lattice *h, int32_t *spin, int64_t n);
+/* fill the lattice on the device with seeded values uniform in lo..hi:
+   site s (= id-1) gets lo + ((hi-lo+1) * x) >> 32 for the Philox word x of
+   stream 3, counter (s>>1, s>>33, 0, 0), word 2*(s&1) - the role of
+   `set site range lo hi` (src/set.cpp:582-760) without a host array */
+int spkgpu_init_spins(spkgpu_lattice *h, int32_t lo, int32_t hi);
 /* per-site Park-Miller states for SPKGPU_RNG_STRICT (AppLattice::siteseeds) */
 int spkgpu_upload_siteseeds(spkgpu_lattice *h, const int32_t *seeds, int64_t n);
 int spkgpu_download_siteseeds(spkgpu_lattice *h, int32_t *seeds, int64_t n);

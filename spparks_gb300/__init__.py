@@ -92,7 +92,7 @@ class EnsembleStats(ctypes.Structure):
 # every symbol include/spkgpu.h (and the other include/*.h) declares
 EXPORTS = [
     "spkgpu_create", "spkgpu_destroy", "spkgpu_last_error", "spkgpu_version", "spkgpu_set_temperature",
-    "spkgpu_upload_spins", "spkgpu_download_spins", "spkgpu_upload_siteseeds", "spkgpu_download_siteseeds",
+    "spkgpu_upload_spins", "spkgpu_download_spins", "spkgpu_init_spins", "spkgpu_upload_siteseeds", "spkgpu_download_siteseeds",
     "spkgpu_upload_mask", "spkgpu_download_mask", "spkgpu_sweep", "spkgpu_set_sweep_index",
     "spkgpu_get_stats", "spkgpu_energy", "spkgpu_synchronize", "spkgpu_timed_sweeps", "spkgpu_stream",
     "spkgpu_device_spins", "spkgpu_launch_count", "spkgpu_kmc_setup", "spkgpu_kmc_run",
@@ -121,6 +121,7 @@ def load_library(path: Path | None = None):
     L.spkgpu_last_error.argtypes = [vp]
     L.spkgpu_last_error.restype = ctypes.c_char_p
     L.spkgpu_set_temperature.argtypes = [vp, ctypes.c_double]
+    L.spkgpu_init_spins.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
     for name in ("spkgpu_upload_spins", "spkgpu_download_spins", "spkgpu_upload_siteseeds",
                  "spkgpu_download_siteseeds"):
         getattr(L, name).argtypes = [vp, P(ctypes.c_int32), ctypes.c_int64]
@@ -211,6 +212,10 @@ class Lattice:
     def upload(self, spin: np.ndarray):
         s = np.ascontiguousarray(spin, dtype=np.int32)
         self._check(self.lib.spkgpu_upload_spins(self.h, _i32p(s), s.size))
+
+    def init_spins(self, lo: int = 1, hi: int | None = None):
+        """Seeded values lo..hi generated on the device (Philox init stream)."""
+        self._check(self.lib.spkgpu_init_spins(self.h, int(lo), int(self.desc.nspins if hi is None else hi)))
 
     def download(self, out: np.ndarray | None = None) -> np.ndarray:
         out = np.empty(self.n, dtype=np.int32) if out is None else out

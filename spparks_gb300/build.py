@@ -26,6 +26,7 @@ SOURCES = [
     "kmc.cu",
     "ensemble.cu",
     "noalloc.cu",
+    "packed.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

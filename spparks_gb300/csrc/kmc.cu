@@ -464,6 +464,7 @@ extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, 
   if (!h) return SPKGPU_ERR_ARG;
   const spkgpu_desc &d = h->d;
   if (d.nsector < 2) return spk_fail(h, SPKGPU_ERR_UNSUPPORTED, "KMC on the GPU needs sectors (sector yes|2|4|8)");
+  if (h->packed) return spk_fail(h, SPKGPU_ERR_UNSUPPORTED, "KMC needs one value per site (spin_bytes 1, 2 or 4)");
   if (d.rng != SPKGPU_RNG_PHILOX) return spk_fail(h, SPKGPU_ERR_ARG, "KMC uses Philox draws");
   if (adapt && !(nstop > 0.0)) return spk_fail(h, SPKGPU_ERR_ARG, "nstop must be > 0");
   if (!adapt && !(tstop > 0.0)) return spk_fail(h, SPKGPU_ERR_ARG, "tstop must be > 0");

@@ -1,0 +1,179 @@
+// Bit-packed (multispin) Ising on sc/6n: 64 sites per uint64, bit b of word
+// (w, y, z) holds site x = 64w + b as (value - 1).  Same per-site rule and
+// Philox draws as the int8/int16/int32 path (AppIsing::site_event_rejection,
+// src/app_ising.cpp:104-136; colours of Lattice::id2color SC_6N,
+// src/lattice.cpp:256-260), so the lattices are bit-identical.
+//
+// Per sweep:
+//   packed_draw_kernel   one thread per word computes the Philox block of
+//                        each of its 32 x-pairs once and stores, for all 64
+//                        sites, four decision masks: the proposal (draw 0 >=
+//                        2^31-1 proposes value 2) and "draw 1 < thr[dE]" for
+//                        the three uphill moves dE = 2, 4, 6.
+//   packed_phase_kernel  per colour, one thread per word: the unlike count of
+//                        every site against its six neighbours as a
+//                        bit-sliced 3-bit sum of XOR masks; a site of the
+//                        colour flips when its proposal differs from it and
+//                        e0 >= 3 (dE <= 0) or the stored decision for
+//                        dE = 6 - 2*e0 holds.  Words are updated in place:
+//                        a colour's bits never neighbour each other, so
+//                        concurrent readers only use bits that do not change.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "site_update.cuh"
+#include "spk_internal.h"
+
+namespace spk {
+
+struct PackedDecisions {
+  uint64_t prop, a2, a4, a6;
+};
+
+__global__ void packed_draw_kernel(const PackedArgs a) {
+  int64_t nw = a.nwords;
+  int64_t words_per_row = a.nx >> 6;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nw; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t row = t / words_per_row;
+    int64_t w = t - row * words_per_row;
+    int64_t s0 = row * a.nx + (w << 6);  // site of bit 0 (even)
+    uint64_t prop = 0, a2 = 0, a4 = 0, a6 = 0;
+#pragma unroll 4
+    for (int m = 0; m < 32; m++) {
+      int64_t s = s0 + 2 * m;
+      U4 q = philox4x32_10(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), a.sweep, 0u}, a.seed, kStreamSweep);
+      uint64_t be = 1ull << (2 * m), bo = be << 1;
+      prop |= (q.x >= 0x7FFFFFFFu ? be : 0) | (q.z >= 0x7FFFFFFFu ? bo : 0);
+      a2 |= ((uint64_t)q.y < a.thr2 ? be : 0) | ((uint64_t)q.w < a.thr2 ? bo : 0);
+      a4 |= ((uint64_t)q.y < a.thr4 ? be : 0) | ((uint64_t)q.w < a.thr4 ? bo : 0);
+      a6 |= ((uint64_t)q.y < a.thr6 ? be : 0) | ((uint64_t)q.w < a.thr6 ? bo : 0);
+    }
+    PackedDecisions *D = (PackedDecisions *)a.decisions;
+    D[t] = PackedDecisions{prop, a2, a4, a6};
+  }
+}
+
+__global__ void packed_phase_kernel(const PackedArgs a, int color) {
+  uint64_t *W = (uint64_t *)a.words;
+  const PackedDecisions *D = (const PackedDecisions *)a.decisions;
+  int64_t words_per_row = a.nx >> 6;
+  int64_t nw = a.nwords;
+  unsigned long long flips = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nw; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t row = t / words_per_row;
+    int w = (int)(t - row * words_per_row);
+    int y = (int)(row % a.ny);
+    int z = (int)(row / a.ny);
+    // colour of bit b: (x + y + z) even -> colour 1; x parity = bit parity
+    uint64_t cmask = (((color - 1 + y + z) & 1) == 0) ? 0x5555555555555555ull : 0xAAAAAAAAAAAAAAAAull;
+    uint64_t s = W[t];
+    int wm = w == 0 ? (int)words_per_row - 1 : w - 1;
+    int wp = w == (int)words_per_row - 1 ? 0 : w + 1;
+    uint64_t xm = (s << 1) | (W[row * words_per_row + wm] >> 63);
+    uint64_t xp = (s >> 1) | (W[row * words_per_row + wp] << 63);
+    int ym = y == 0 ? a.ny - 1 : y - 1, yp = y == a.ny - 1 ? 0 : y + 1;
+    int zm = z == 0 ? a.nz - 1 : z - 1, zp = z == a.nz - 1 ? 0 : z + 1;
+    uint64_t nym = W[((int64_t)z * a.ny + ym) * words_per_row + w];
+    uint64_t nyp = W[((int64_t)z * a.ny + yp) * words_per_row + w];
+    uint64_t nzm = W[((int64_t)zm * a.ny + y) * words_per_row + w];
+    uint64_t nzp = W[((int64_t)zp * a.ny + y) * words_per_row + w];
+    // bit-sliced count of unlike neighbours: e0 = b2 b1 b0 (0..6)
+    uint64_t d[6] = {s ^ xm, s ^ nym, s ^ nyp, s ^ nzm, s ^ nzp, s ^ xp};
+    uint64_t b0 = 0, b1 = 0, b2 = 0;
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      uint64_t c0 = b0 & d[j];
+      b0 ^= d[j];
+      uint64_t c1 = b1 & c0;
+      b1 ^= c0;
+      b2 |= c1;
+    }
+    PackedDecisions dd = D[t];
+    uint64_t ge3 = b2 | (b1 & b0);                 // e0 >= 3: downhill or level
+    uint64_t e2 = ~b2 & b1 & ~b0;                  // dE = 2
+    uint64_t e1 = ~b2 & ~b1 & b0;                  // dE = 4
+    uint64_t e0z = ~b2 & ~b1 & ~b0;                // dE = 6
+    uint64_t accept = ge3 | (e2 & dd.a2) | (e1 & dd.a4) | (e0z & dd.a6);
+    uint64_t flip = (dd.prop ^ s) & cmask & accept;
+    if (flip) W[t] = s ^ flip;
+    flips += __popcll(flip);
+  }
+  for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(0xFFFFFFFFu, flips, o);
+  if ((threadIdx.x & 31) == 0 && flips) atomicAdd(a.naccept, flips);
+}
+
+// int32 site values (1 or 2) -> bits; sets *bad on any other value
+__global__ void packed_pack_kernel(const int32_t *src, uint64_t *dst, int64_t nwords, int *bad) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nwords; t += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t v = 0;
+    const int32_t *p = src + (t << 6);
+    for (int b = 0; b < 64; b++) {
+      int s = p[b];
+      if (s < 1 || s > 2) *bad = 1;
+      v |= (uint64_t)(s == 2) << b;
+    }
+    dst[t] = v;
+  }
+}
+
+__global__ void packed_unpack_kernel(const uint64_t *src, int32_t *dst, int64_t nwords) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nwords; t += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t v = src[t];
+    int32_t *p = dst + (t << 6);
+    for (int b = 0; b < 64; b++) p[b] = 1 + (int)((v >> b) & 1);
+  }
+}
+
+// total energy: sum over sites of unlike neighbours = 2 * unlike bonds
+__global__ void packed_energy_kernel(const uint64_t *W, int nx, int ny, int nz, int64_t nwords,
+                                     unsigned long long *out) {
+  int64_t words_per_row = nx >> 6;
+  unsigned long long e = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nwords; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t row = t / words_per_row;
+    int w = (int)(t - row * words_per_row);
+    int y = (int)(row % ny), z = (int)(row / ny);
+    uint64_t s = W[t];
+    int wp = w == (int)words_per_row - 1 ? 0 : w + 1;
+    uint64_t xp = (s >> 1) | (W[row * words_per_row + wp] << 63);
+    int yp = y == ny - 1 ? 0 : y + 1, zp = z == nz - 1 ? 0 : z + 1;
+    uint64_t nyp = W[((int64_t)z * ny + yp) * words_per_row + w];
+    uint64_t nzp = W[((int64_t)zp * ny + y) * words_per_row + w];
+    e += 2ull * (__popcll(s ^ xp) + __popcll(s ^ nyp) + __popcll(s ^ nzp));
+  }
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xFFFFFFFFu, e, o);
+  if ((threadIdx.x & 31) == 0 && e) atomicAdd(out, e);
+}
+
+static unsigned grid_for(int64_t n, int sms, int per_sm = 8) {
+  int64_t b = (n + 255) / 256;
+  int64_t cap = (int64_t)sms * per_sm;
+  return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+cudaError_t launch_packed_sweep(const PackedArgs &a, cudaStream_t s, int num_sms) {
+  packed_draw_kernel<<<grid_for(a.nwords, num_sms), 256, 0, s>>>(a);
+  packed_phase_kernel<<<grid_for(a.nwords, num_sms), 256, 0, s>>>(a, 1);
+  packed_phase_kernel<<<grid_for(a.nwords, num_sms), 256, 0, s>>>(a, 2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_packed_pack(const int32_t *src, uint64_t *dst, int64_t nwords, int *bad, cudaStream_t s, int num_sms) {
+  packed_pack_kernel<<<grid_for(nwords, num_sms), 256, 0, s>>>(src, dst, nwords, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_packed_unpack(const uint64_t *src, int32_t *dst, int64_t nwords, cudaStream_t s, int num_sms) {
+  packed_unpack_kernel<<<grid_for(nwords, num_sms), 256, 0, s>>>(src, dst, nwords);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_packed_energy(const uint64_t *W, int nx, int ny, int nz, unsigned long long *out, cudaStream_t s,
+                                 int num_sms) {
+  int64_t nw = (int64_t)(nx >> 6) * ny * nz;
+  packed_energy_kernel<<<grid_for(nw, num_sms), 256, 0, s>>>(W, nx, ny, nz, nw, out);
+  return cudaGetLastError();
+}
+
+}  // namespace spk

@@ -96,6 +96,8 @@ cudaError_t launch_convert_in(int spin_bytes, const int32_t *src, void *dst, int
                               int *bad, cudaStream_t s);
 cudaError_t launch_convert_out(int spin_bytes, const void *src, int32_t *dst, int64_t n,
                                cudaStream_t s);
+cudaError_t launch_init(int spin_bytes, void *dst, int64_t n, uint32_t seed, int lo, int hi, cudaStream_t s,
+                        int num_sms);
 
 // fused whole-sweep tile kernel for 2d lattices without sectors
 // (returns cudaErrorNotSupported when the configuration is not covered)
@@ -111,6 +113,23 @@ struct FusedArgs {
 bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny);
 cudaError_t launch_fused2d(int lattice, int app, int spin_bytes, const FusedArgs &a, cudaStream_t s,
                            int num_sms);
+
+// bit-packed Ising on sc/6n (packed.cu)
+struct PackedArgs {
+  void *words;                 // nx/64 * ny * nz uint64
+  void *decisions;             // 4 uint64 per word
+  int nx, ny, nz;
+  int64_t nwords;
+  uint32_t seed, sweep;
+  uint64_t thr2, thr4, thr6;   // Boltzmann thresholds for dE = 2, 4, 6
+  unsigned long long *naccept;
+};
+cudaError_t launch_packed_sweep(const PackedArgs &a, cudaStream_t s, int num_sms);
+cudaError_t launch_packed_pack(const int32_t *src, uint64_t *dst, int64_t nwords, int *bad, cudaStream_t s,
+                               int num_sms);
+cudaError_t launch_packed_unpack(const uint64_t *src, int32_t *dst, int64_t nwords, cudaStream_t s, int num_sms);
+cudaError_t launch_packed_energy(const uint64_t *W, int nx, int ny, int nz, unsigned long long *out, cudaStream_t s,
+                                 int num_sms);
 
 }  // namespace spk
 
@@ -132,6 +151,8 @@ struct spkgpu_lattice {
   int num_sms = 0;
   void *d_spin = nullptr;
   void *d_spin_alt = nullptr;   // second buffer of the fused double-buffered sweep
+  void *d_decisions = nullptr;  // bit-packed path: per-word decision masks of a sweep
+  bool packed = false;          // spin_bytes == -1: 64 Ising sites per uint64
   int32_t *d_seeds = nullptr;
   uint8_t *d_mask = nullptr;
   unsigned long long *d_counters = nullptr;  // [0] naccept, [1] energy, [2] flags

@@ -153,13 +153,21 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
   if (d.nx % 2 || d.ny % 2 || (!spk::is2d(d.lattice) && d.nz % 2)) return SPKGPU_ERR_ARG;
   int sb = d.spin_bytes;
   if (sb == 0) sb = d.nspins <= 127 ? 1 : (d.nspins <= 32767 ? 2 : 4);
-  if (!(sb == 1 || sb == 2 || sb == 4)) return SPKGPU_ERR_ARG;
+  bool packed = (sb == -1);
+  if (packed) {  // multispin Ising: sc/6n, 64 sites of x per word, plain colour sweeps
+    if (d.lattice != SPKGPU_SC_6N || d.app != SPKGPU_ISING || d.nx % 64 || d.nsector != 1 || d.nloop != 1 ||
+        d.rng != SPKGPU_RNG_PHILOX || d.mask || d.variant != 0)
+      return SPKGPU_ERR_ARG;
+  } else if (!(sb == 1 || sb == 2 || sb == 4)) {
+    return SPKGPU_ERR_ARG;
+  }
   if ((sb == 1 && d.nspins > 127) || (sb == 2 && d.nspins > 32767)) return SPKGPU_ERR_ARG;
 
   spkgpu_lattice *h = new (std::nothrow) spkgpu_lattice();
   if (!h) return SPKGPU_ERR_NOMEM;
   h->d = d;
   h->spin_bytes = sb;
+  h->packed = packed;
   h->n = (int64_t)d.nx * d.ny * d.nz;
   h->ncolors = spk::ncolors_of(d.lattice);
   h->maxneigh = spk::maxneigh_of(d.lattice);
@@ -178,8 +186,10 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
   if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
     return fail(SPKGPU_ERR_CUDA);
-  if (cudaMalloc(&h->d_spin, (size_t)h->n * sb) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
-  if (cudaMemsetAsync(h->d_spin, 0, (size_t)h->n * sb, h->stream) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
+  size_t spin_alloc = packed ? (size_t)h->n / 8 : (size_t)h->n * sb;
+  if (cudaMalloc(&h->d_spin, spin_alloc) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
+  if (cudaMemsetAsync(h->d_spin, 0, spin_alloc, h->stream) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
+  if (packed && cudaMalloc(&h->d_decisions, (size_t)h->n / 64 * 32) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
   if (cudaMalloc(&h->d_counters, 8 * sizeof(unsigned long long)) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
   cudaMemsetAsync(h->d_counters, 0, 8 * sizeof(unsigned long long), h->stream);
   if (d.rng == SPKGPU_RNG_STRICT) {
@@ -219,7 +229,7 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
     return fail(SPKGPU_ERR_CUDA);
   }
   h->axes = ax;
-  h->fused_ok = (d.variant == 0 && d.nsector == 1 && d.nloop == 1 &&
+  h->fused_ok = (!packed && d.variant == 0 && d.nsector == 1 && d.nloop == 1 &&
                  d.rng == SPKGPU_RNG_PHILOX && !d.mask &&
                  spk::fused2d_supported(d.lattice, d.app, sb, d.nx, d.ny));
   if (h->fused_ok) {
@@ -236,6 +246,7 @@ int spkgpu_destroy(spkgpu_lattice *h) {
   spk_kmc_free(h);
   cudaFree(h->d_spin);
   cudaFree(h->d_spin_alt);
+  cudaFree(h->d_decisions);
   cudaFree(h->d_seeds);
   cudaFree(h->d_mask);
   cudaFree(h->d_counters);
@@ -282,14 +293,29 @@ int spkgpu_upload_spins(spkgpu_lattice *h, const int32_t *spin, int64_t n) {
   for (int64_t off = 0; off < n; off += kStageChunk) {
     int64_t m = std::min(kStageChunk, n - off);
     SPK_CUDA(h, cudaMemcpyAsync(h->d_stage, spin + off, (size_t)m * 4, cudaMemcpyHostToDevice, h->stream));
-    SPK_CUDA(h, spk::launch_convert_in(h->spin_bytes, h->d_stage, (char *)h->d_spin + off * h->spin_bytes, m,
-                                       h->d.nspins, bad, h->stream));
+    if (h->packed)
+      SPK_CUDA(h, spk::launch_packed_pack(h->d_stage, (uint64_t *)h->d_spin + off / 64, m / 64, bad, h->stream,
+                                          h->num_sms));
+    else
+      SPK_CUDA(h, spk::launch_convert_in(h->spin_bytes, h->d_stage, (char *)h->d_spin + off * h->spin_bytes, m,
+                                         h->d.nspins, bad, h->stream));
     h->launches++;
   }
   int badh = 0;
   SPK_CUDA(h, cudaMemcpyAsync(&badh, bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   SPK_CUDA(h, cudaStreamSynchronize(h->stream));
   if (badh) return spk_fail(h, SPKGPU_ERR_INVALID_SPIN, "One or more sites have invalid values");
+  return SPKGPU_OK;
+}
+
+int spkgpu_init_spins(spkgpu_lattice *h, int32_t lo, int32_t hi) {
+  if (!h) return SPKGPU_ERR_ARG;
+  if (lo < 1 || hi < lo || hi > h->d.nspins) return spk_fail(h, SPKGPU_ERR_ARG, "values must lie in 1..nspins");
+  if (h->packed && (lo != 1 || hi != 2)) return spk_fail(h, SPKGPU_ERR_ARG, "packed lattices take 1..2");
+  SPK_CUDA(h, spk::launch_init(h->packed ? -1 : h->spin_bytes, h->d_spin, h->n, h->d.seed, lo, hi, h->stream,
+                               h->num_sms));
+  h->launches++;
+  SPK_CUDA(h, cudaStreamSynchronize(h->stream));
   return SPKGPU_OK;
 }
 
@@ -300,8 +326,12 @@ int spkgpu_download_spins(spkgpu_lattice *h, int32_t *spin, int64_t n) {
   if (rc) return rc;
   for (int64_t off = 0; off < n; off += kStageChunk) {
     int64_t m = std::min(kStageChunk, n - off);
-    SPK_CUDA(h, spk::launch_convert_out(h->spin_bytes, (const char *)h->d_spin + off * h->spin_bytes, h->d_stage, m,
-                                        h->stream));
+    if (h->packed)
+      SPK_CUDA(h, spk::launch_packed_unpack((const uint64_t *)h->d_spin + off / 64, h->d_stage, m / 64, h->stream,
+                                            h->num_sms));
+    else
+      SPK_CUDA(h, spk::launch_convert_out(h->spin_bytes, (const char *)h->d_spin + off * h->spin_bytes, h->d_stage,
+                                          m, h->stream));
     h->launches++;
     SPK_CUDA(h, cudaMemcpyAsync(spin + off, h->d_stage, (size_t)m * 4, cudaMemcpyDeviceToHost, h->stream));
   }
@@ -360,7 +390,23 @@ static int enqueue_sweeps(spkgpu_lattice *h, int32_t nsweeps) {
   int nsec = d.nsector;
   for (int32_t s = 0; s < nsweeps; s++) {
     uint32_t sweep = (uint32_t)h->sweep;
-    if (h->fused_ok) {
+    if (h->packed) {
+      spk::PackedArgs pa;
+      pa.words = h->d_spin;
+      pa.decisions = h->d_decisions;
+      pa.nx = d.nx;
+      pa.ny = d.ny;
+      pa.nz = d.nz;
+      pa.nwords = h->n / 64;
+      pa.seed = d.seed;
+      pa.sweep = sweep;
+      pa.thr2 = h->acc.thr[2];
+      pa.thr4 = h->acc.thr[4];
+      pa.thr6 = h->acc.thr[6];
+      pa.naccept = nacc;
+      SPK_CUDA(h, spk::launch_packed_sweep(pa, h->stream, h->num_sms));
+      h->launches += 3;
+    } else if (h->fused_ok) {
       spk::FusedArgs f;
       f.src = h->d_spin;
       f.dst = h->d_spin_alt;
@@ -506,8 +552,12 @@ int spkgpu_energy(spkgpu_lattice *h, double *energy) {
   if (!h || !energy) return SPKGPU_ERR_ARG;
   unsigned long long *acc = h->d_counters + 1;
   SPK_CUDA(h, cudaMemsetAsync(acc, 0, sizeof(unsigned long long), h->stream));
-  SPK_CUDA(h, spk::launch_energy(h->d.lattice, h->spin_bytes, h->d_spin, h->d.nx, h->d.ny, h->d.nz, acc,
-                                 h->stream, h->num_sms));
+  if (h->packed)
+    SPK_CUDA(h, spk::launch_packed_energy((const uint64_t *)h->d_spin, h->d.nx, h->d.ny, h->d.nz, acc, h->stream,
+                                          h->num_sms));
+  else
+    SPK_CUDA(h, spk::launch_energy(h->d.lattice, h->spin_bytes, h->d_spin, h->d.nx, h->d.ny, h->d.nz, acc,
+                                   h->stream, h->num_sms));
   h->launches++;
   unsigned long long e = 0;
   SPK_CUDA(h, cudaMemcpyAsync(&e, acc, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
@@ -531,7 +581,7 @@ int spkgpu_stream(spkgpu_lattice *h, void **stream) {
 int spkgpu_device_spins(spkgpu_lattice *h, void **dptr, int64_t *bytes) {
   if (!h || !dptr || !bytes) return SPKGPU_ERR_ARG;
   *dptr = h->d_spin;
-  *bytes = h->n * h->spin_bytes;
+  *bytes = h->packed ? h->n / 8 : h->n * h->spin_bytes;
   return SPKGPU_OK;
 }
 

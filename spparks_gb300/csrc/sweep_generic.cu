@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "site_update.cuh"
 #include "spk_internal.h"
 
@@ -284,6 +286,38 @@ cudaError_t launch_convert_out(int spin_bytes, const void *src, int32_t *dst, in
     case 1: convert_out_kernel<int8_t><<<(unsigned)blocks, 256, 0, s>>>((const int8_t *)src, dst, n); break;
     case 2: convert_out_kernel<int16_t><<<(unsigned)blocks, 256, 0, s>>>((const int16_t *)src, dst, n); break;
     case 4: convert_out_kernel<int32_t><<<(unsigned)blocks, 256, 0, s>>>((const int32_t *)src, dst, n); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// seeded initial values: site s gets init_spin(seed, s, lo, hi), the Philox
+// init stream (the role of `set site range lo hi`, src/set.cpp:582-760)
+
+template <typename S>
+__global__ void init_kernel(S *dst, int64_t n, uint32_t seed, int lo, int hi) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (S)init_spin(seed, (uint64_t)i, lo, hi);
+}
+
+__global__ void init_packed_kernel(uint64_t *dst, int64_t nwords, uint32_t seed) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nwords; t += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t v = 0;
+    for (int b = 0; b < 64; b++) v |= (uint64_t)(init_spin(seed, (uint64_t)(t * 64 + b), 1, 2) == 2) << b;
+    dst[t] = v;
+  }
+}
+
+cudaError_t launch_init(int spin_bytes, void *dst, int64_t n, uint32_t seed, int lo, int hi, cudaStream_t s,
+                        int num_sms) {
+  int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)num_sms * 16);
+  if (blocks < 1) blocks = 1;
+  switch (spin_bytes) {
+    case 1: init_kernel<int8_t><<<(unsigned)blocks, 256, 0, s>>>((int8_t *)dst, n, seed, lo, hi); break;
+    case 2: init_kernel<int16_t><<<(unsigned)blocks, 256, 0, s>>>((int16_t *)dst, n, seed, lo, hi); break;
+    case 4: init_kernel<int32_t><<<(unsigned)blocks, 256, 0, s>>>((int32_t *)dst, n, seed, lo, hi); break;
+    case -1: init_packed_kernel<<<(unsigned)blocks, 256, 0, s>>>((uint64_t *)dst, n / 64, seed); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
