@@ -109,10 +109,47 @@ __device__ __forceinline__ int replica_of_tile(const int32_t *tile_start, int nr
   return lo;
 }
 
+// walks the tiles of a contiguous range, keeping the current replica's
+// parameters in registers; replica = temperature index of the tile's replica
+// (the thresholds are indexed by temperature)
+struct ReplicaCursor {
+  int r = 0, tend = 0, L = 0, tpr = 1, tbeg = 0, tidx = 0;
+  int64_t base = 0;
+  __device__ void load(const EnsArgs &a, int rr) {
+    r = rr;
+    tbeg = a.tile_start[r];
+    tend = a.tile_start[r + 1];
+    L = a.L[r];
+    tpr = L / kTile;
+    base = a.base[r];
+    tidx = a.tidx[r];
+  }
+  __device__ void seek(const EnsArgs &a, int t) { load(a, replica_of_tile(a.tile_start, a.nrep, t)); }
+  template <typename S>
+  __device__ void job(const EnsArgs &a, int t, const void *src, void *dst, uint32_t sweep, TileJob *j) {
+    while (t >= tend) load(a, r + 1);
+    int lt = t - tbeg;
+    j->src = (const S *)src + base;
+    j->dst = (S *)dst + base;
+    j->L = L;
+    j->Ly = L;
+    j->x0 = (lt % tpr) * kTile;
+    j->y0 = (lt / tpr) * kTile;
+    j->base = 0;  // replicas differ by Philox stream word; site counter is local
+    j->seed = a.seed;
+    j->key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
+    j->sweep = sweep;
+    j->nspins = a.nspins;
+    j->replica = tidx;
+    j->zero_t = 0;
+    j->thr = nullptr;
+  }
+};
+
 template <int APP, typename S>
-__global__ void __launch_bounds__(kTileThreads) ensemble_kernel(EnsArgs a) {
-  __shared__ S stage[kStage * kStage];
-  __shared__ uint64_t thr[5];
+__global__ void __launch_bounds__(kTileThreads, 8) ensemble_kernel(EnsArgs a) {
+  __shared__ __align__(16) S stage[3][kStageSites];
+  __shared__ uint64_t thr[3][5];
   __shared__ unsigned long long red[kTileThreads / 32];
   EnsCtl *ctl = a.ctl;
   int parity = *(volatile int *)&ctl->parity;
@@ -123,42 +160,54 @@ __global__ void __launch_bounds__(kTileThreads) ensemble_kernel(EnsArgs a) {
   for (int s = 0; s < a.nsweeps && ok; s++) {
     const void *src = parity ? a.buf1 : a.buf0;
     void *dst = parity ? a.buf0 : a.buf1;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-      int r = replica_of_tile(a.tile_start, a.nrep, t);
-      int L = a.L[r];
-      int tpr = L / kTile;
-      int lt = t - a.tile_start[r];
-      if (threadIdx.x < 5) thr[threadIdx.x] = a.thr[(int64_t)a.tidx[r] * 5 + threadIdx.x];
-      TileJob j;
-      j.src = (const S *)src + a.base[r];
-      j.dst = (S *)dst + a.base[r];
-      j.L = L;
-      j.Ly = L;
-      j.x0 = (lt % tpr) * kTile;
-      j.y0 = (lt / tpr) * kTile;
-      j.base = 0;  // replicas differ by Philox stream word; site counter is local
-      j.seed = a.seed;
-      j.key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
-      j.sweep = sweep0 + (uint32_t)s;
-      j.nspins = a.nspins;
-      j.zero_t = 0;
-      j.thr = thr;
-      my_changed += (unsigned long long)tile_sweep_sq4<APP, S>(j, stage);
+    // each CTA sweeps a contiguous range of tiles (all tiles cost the same),
+    // so consecutive tiles almost always share a replica and its parameters
+    // are looked up only when the replica changes.  Software pipeline: tile
+    // t+1 is staged (cp.async) into the next of three buffers while tile t is
+    // swept; by the time a buffer is staged again every thread has passed the
+    // barriers of the tile in between, so no thread still reads it.
+    const int t0 = (int)(((int64_t)a.ntiles * blockIdx.x) / gridDim.x);
+    const int t1 = (int)(((int64_t)a.ntiles * (blockIdx.x + 1)) / gridDim.x);
+    const uint32_t sweep = sweep0 + (uint32_t)s;
+    ReplicaCursor rc;
+    if (t0 < t1) rc.seek(a, t0);
+    TileJob cur, nxt;
+    int sb = 0;
+    if (t0 < t1) {
+      rc.job<S>(a, t0, src, dst, sweep, &cur);
+      tile_stage_async<S>(cur, stage[sb]);
     }
+    cp_async_commit();
+    for (int t = t0; t < t1; t++) {
+      int sn = sb == 2 ? 0 : sb + 1;
+      if (threadIdx.x < 5) thr[sb][threadIdx.x] = a.thr[(int64_t)cur.replica * 5 + threadIdx.x];
+      if (t + 1 < t1) {
+        rc.job<S>(a, t + 1, src, dst, sweep, &nxt);
+        tile_stage_async<S>(nxt, stage[sn]);
+      }
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+      cur.thr = thr[sb];
+      my_changed += (unsigned long long)tile_sweep_sq4<APP, S>(cur, stage[sb]);
+      cur = nxt;
+      sb = sn;
+    }
+    cp_async_wait<0>();
     parity ^= 1;
     ok = grid_barrier(ctl);
     if (!ok) break;
     uint32_t done = sweep0 + (uint32_t)s + 1;
     if (a.exchange_every > 0 && done % (uint32_t)a.exchange_every == 0) {
       // unlike bonds of each replica (right and down neighbour of each site)
-      const S *cur = (const S *)(parity ? a.buf1 : a.buf0);
+      const S *curbuf = (const S *)(parity ? a.buf1 : a.buf0);
       for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         int r = replica_of_tile(a.tile_start, a.nrep, t);
         int L = a.L[r];
         int tpr = L / kTile;
         int lt = t - a.tile_start[r];
         int x0 = (lt % tpr) * kTile, y0 = (lt / tpr) * kTile;
-        const S *rep = cur + a.base[r];
+        const S *rep = curbuf + a.base[r];
         unsigned int b = 0;
         for (int k = threadIdx.x; k < kTile * kTile; k += kTileThreads) {
           int y = y0 + (k >> 5), x = x0 + (k & 31);

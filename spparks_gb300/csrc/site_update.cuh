@@ -112,7 +112,8 @@ __device__ __forceinline__ int update_philox(int own, const int (&nb)[NN], uint3
     news = pick_value<NN>(nb, j);
   }
   if (news == own) return own;
-  int e1 = count_unlike<NN>(news, nb);
+  // two-state Ising: every neighbour equals either own or news
+  int e1 = (APP == SPKGPU_ISING) ? NN - e0 : count_unlike<NN>(news, nb);
   if (e1 <= e0) return news;
   if (zero_t) return own;
   return ((uint64_t)x1 < thr[e1 - e0]) ? news : own;

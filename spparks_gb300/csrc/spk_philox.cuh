@@ -42,15 +42,11 @@ struct U4 {
   uint32_t x, y, z, w;
 };
 
+// one 32x32->64 multiply (a single IMAD.WIDE.U32 on the device)
 SPK_HD void mulhilo(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
-#ifdef __CUDA_ARCH__
-  lo = a * b;
-  hi = __umulhi(a, b);
-#else
   uint64_t p = (uint64_t)a * b;
   lo = (uint32_t)p;
   hi = (uint32_t)(p >> 32);
-#endif
 }
 
 SPK_HD U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
@@ -69,6 +65,43 @@ SPK_HD U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
     c = n;
     k0 += kPhiloxW0;
     k1 += kPhiloxW1;
+  }
+  return c;
+}
+
+// the ten round keys of a key, for callers that draw many blocks with one key
+struct RoundKeys {
+  uint32_t k0[10], k1[10];
+};
+
+SPK_HD RoundKeys round_keys(uint32_t k0, uint32_t k1) {
+  RoundKeys r;
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+  for (int i = 0; i < 10; i++) {
+    r.k0[i] = k0;
+    r.k1[i] = k1;
+    k0 += kPhiloxW0;
+    k1 += kPhiloxW1;
+  }
+  return r;
+}
+
+SPK_HD U4 philox4x32_10_rk(U4 c, const RoundKeys &rk) {
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo(kPhiloxM0, c.x, hi0, lo0);
+    mulhilo(kPhiloxM1, c.z, hi1, lo1);
+    U4 n;
+    n.x = hi1 ^ c.y ^ rk.k0[r];
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ rk.k1[r];
+    n.w = lo0;
+    c = n;
   }
   return c;
 }

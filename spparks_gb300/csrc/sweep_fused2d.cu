@@ -11,7 +11,7 @@ namespace spk {
 
 template <int APP, typename S>
 __global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
-  __shared__ S stage[kStage * kStage];
+  __shared__ __align__(16) S stage[kStageSites];
   __shared__ uint64_t thr[5];
   if (threadIdx.x < 5) thr[threadIdx.x] = a.acc.thr[threadIdx.x];
   int tpr = a.nx / kTile;
@@ -27,8 +27,13 @@ __global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
   j.key1 = kStreamSweep;
   j.sweep = a.sweep;
   j.nspins = a.nspins;
+  j.replica = 0;
   j.zero_t = a.acc.zero_t;
   j.thr = thr;
+  tile_stage_async<S>(j, stage);
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
   int changed = tile_sweep_sq4<APP, S>(j, stage);
   unsigned int w = __reduce_add_sync(0xFFFFFFFFu, (unsigned)changed);
   if ((threadIdx.x & 31) == 0 && w) atomicAdd(a.naccept, (unsigned long long)w);
