@@ -162,7 +162,7 @@ int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_
    spin_bytes each (1, 2 or 4; row-major, site index = id-1) and is updated in
    place; nx and ny must be multiples of 32.  Sweep k uses Philox sweep index
    sweep0+k.  The second sweep buffer and the change counter come from one
-   static device array of SPKGPU_NOALLOC_MAX_BYTES (+256) bytes that every
+   static device array of SPKGPU_NOALLOC_MAX_BYTES (+2048) bytes that every
    GPU loading the library holds until exit; larger lattices return
    SPKGPU_ERR_TOO_LARGE.  The array is shared by all calls and keeps the last
    call's contents, so calls whose GPU work overlaps race: serialise them.

@@ -27,6 +27,7 @@ SOURCES = [
     "ensemble.cu",
     "noalloc.cu",
     "packed.cu",
+    "sweep_rows.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

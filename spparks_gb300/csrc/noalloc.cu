@@ -31,11 +31,13 @@
 
 #include <mutex>
 
+#include "counters.cuh"
 #include "spk_internal.h"
 
 namespace {
 
-constexpr size_t kCounterBytes = 256;  // change counter, padded to keep the buffer aligned
+// change-counter slots (spk::kCounterSlots of 8 bytes), then the buffer
+constexpr size_t kCounterBytes = 2048;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kCounterBytes + SPKGPU_NOALLOC_MAX_BYTES];
 
 constexpr int kMaxDevices = 64;
@@ -82,7 +84,8 @@ extern "C" int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int3
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 
-  if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s) != cudaSuccess) return SPKGPU_ERR_CUDA;
+  static_assert(kCounterBytes == spk::kCounterSlots * sizeof(unsigned long long), "counter slots");
+  if (cudaMemsetAsync(counter, 0, kCounterBytes, s) != cudaSuccess) return SPKGPU_ERR_CUDA;
   spk::FusedArgs f;
   f.nx = nx;
   f.ny = ny;
@@ -101,10 +104,12 @@ extern "C" int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int3
     if (cudaMemcpyAsync(spin, other, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return SPKGPU_ERR_CUDA;
   }
   if (naccept) {
-    unsigned long long v = 0;
-    if (cudaMemcpyAsync(&v, counter, sizeof(v), cudaMemcpyDeviceToHost, s) != cudaSuccess) return SPKGPU_ERR_CUDA;
+    unsigned long long v[spk::kCounterSlots];
+    if (cudaMemcpyAsync(v, counter, sizeof(v), cudaMemcpyDeviceToHost, s) != cudaSuccess) return SPKGPU_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return SPKGPU_ERR_CUDA;
-    *naccept = (int64_t)v;
+    unsigned long long tot = 0;
+    for (int k = 0; k < spk::kCounterSlots; k++) tot += v[k];
+    *naccept = (int64_t)tot;
   }
   return SPKGPU_OK;
 }

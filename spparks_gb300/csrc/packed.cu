@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "counters.cuh"
 #include "site_update.cuh"
 #include "spk_internal.h"
 
@@ -99,8 +100,7 @@ __global__ void packed_phase_kernel(const PackedArgs a, int color) {
     if (flip) W[t] = s ^ flip;
     flips += __popcll(flip);
   }
-  for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(0xFFFFFFFFu, flips, o);
-  if ((threadIdx.x & 31) == 0 && flips) atomicAdd(a.naccept, flips);
+  block_count_add(a.naccept, flips);
 }
 
 // int32 site values (1 or 2) -> bits; sets *bad on any other value

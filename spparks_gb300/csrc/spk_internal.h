@@ -114,6 +114,12 @@ bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny);
 cudaError_t launch_fused2d(int lattice, int app, int spin_bytes, const FusedArgs &a, cudaStream_t s,
                            int num_sms);
 
+// row-pair sweep for sq/8n and sc/26n without sectors (sweep_rows.cu)
+bool rows_supported(int lattice, int spin_bytes, int nx, int nspins);
+cudaError_t launch_rows_sweep(int lattice, int app, int spin_bytes, void *spin, int nx, int ny, int nz,
+                              uint32_t seed, uint32_t sweep, int nspins, unsigned long long *naccept,
+                              const AcceptTable &acc, cudaStream_t st, int *launches);
+
 // bit-packed Ising on sc/6n (packed.cu)
 struct PackedArgs {
   void *words;                 // nx/64 * ny * nz uint64
@@ -171,7 +177,8 @@ struct spkgpu_lattice {
   int64_t nsweeps_done = 0;
   int64_t nattempt = 0;
   int64_t launches = 0;
-  bool fused_ok = false;
+  bool fused_ok = false;         // sq/4n fused tile sweep
+  bool rows_ok = false;          // sq/8n, sc/26n row-pair sweep
   std::string err;
   // KMC state (kmc.cu)
   struct KmcState *kmc = nullptr;

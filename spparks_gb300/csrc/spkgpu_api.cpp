@@ -19,9 +19,15 @@
 #include <string>
 #include <vector>
 
+#include "counters.cuh"
 #include "spk_internal.h"
 
 using spk::AcceptTable;
+
+// d_counters layout: [0,8) scalars ([1] energy, [2] bad-value flag),
+// [8, 8+256) Naccept slots
+static const int kNacceptSlots = 8;
+static const int kCounterWords = kNacceptSlots + spk::kCounterSlots;
 
 int spk_fail(spkgpu_lattice *h, int code, const std::string &msg) {
   if (h) h->err = msg;
@@ -190,8 +196,9 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
   if (cudaMalloc(&h->d_spin, spin_alloc) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
   if (cudaMemsetAsync(h->d_spin, 0, spin_alloc, h->stream) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
   if (packed && cudaMalloc(&h->d_decisions, (size_t)h->n / 64 * 32) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
-  if (cudaMalloc(&h->d_counters, 8 * sizeof(unsigned long long)) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
-  cudaMemsetAsync(h->d_counters, 0, 8 * sizeof(unsigned long long), h->stream);
+  if (cudaMalloc(&h->d_counters, kCounterWords * sizeof(unsigned long long)) != cudaSuccess)
+    return fail(SPKGPU_ERR_NOMEM);
+  cudaMemsetAsync(h->d_counters, 0, kCounterWords * sizeof(unsigned long long), h->stream);
   if (d.rng == SPKGPU_RNG_STRICT) {
     if (cudaMalloc(&h->d_seeds, (size_t)h->n * 4) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
     cudaMemsetAsync(h->d_seeds, 0, (size_t)h->n * 4, h->stream);
@@ -235,6 +242,8 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
   if (h->fused_ok) {
     if (cudaMalloc(&h->d_spin_alt, (size_t)h->n * sb) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
   }
+  h->rows_ok = (!packed && d.variant == 0 && d.nsector == 1 && d.nloop == 1 && d.rng == SPKGPU_RNG_PHILOX &&
+                !d.mask && spk::rows_supported(d.lattice, sb, d.nx, d.nspins));
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
   *out = h;
   return code;
@@ -385,7 +394,7 @@ static int enqueue_sweeps(spkgpu_lattice *h, int32_t nsweeps) {
   const spkgpu_desc &d = h->d;
   spkgpu_axes_store *ax = h->axes;
   const int32_t *A = h->d_axis;
-  unsigned long long *nacc = h->d_counters + 0;
+  unsigned long long *nacc = h->d_counters + kNacceptSlots;
   bool z3 = !spk::is2d(d.lattice);
   int nsec = d.nsector;
   for (int32_t s = 0; s < nsweeps; s++) {
@@ -406,6 +415,11 @@ static int enqueue_sweeps(spkgpu_lattice *h, int32_t nsweeps) {
       pa.naccept = nacc;
       SPK_CUDA(h, spk::launch_packed_sweep(pa, h->stream, h->num_sms));
       h->launches += 3;
+    } else if (h->rows_ok) {
+      int nl = 0;
+      SPK_CUDA(h, spk::launch_rows_sweep(d.lattice, d.app, h->spin_bytes, h->d_spin, d.nx, d.ny, d.nz, d.seed,
+                                         sweep, d.nspins, nacc, h->acc, h->stream, &nl));
+      h->launches += nl;
     } else if (h->fused_ok) {
       spk::FusedArgs f;
       f.src = h->d_spin;
@@ -539,9 +553,12 @@ int spkgpu_timed_sweeps(spkgpu_lattice *h, int32_t nsweeps, float *ms) {
 
 int spkgpu_get_stats(spkgpu_lattice *h, spkgpu_stats *out) {
   if (!h || !out) return SPKGPU_ERR_ARG;
-  unsigned long long na = 0;
-  SPK_CUDA(h, cudaMemcpyAsync(&na, h->d_counters, sizeof(na), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long slots[spk::kCounterSlots];
+  SPK_CUDA(h, cudaMemcpyAsync(slots, h->d_counters + kNacceptSlots, sizeof(slots), cudaMemcpyDeviceToHost,
+                              h->stream));
   SPK_CUDA(h, cudaStreamSynchronize(h->stream));
+  unsigned long long na = 0;
+  for (int k = 0; k < spk::kCounterSlots; k++) na += slots[k];
   out->naccept = (int64_t)na;
   out->nattempt = h->nattempt;
   out->nsweeps = h->nsweeps_done;

@@ -4,6 +4,7 @@
 // lattices without sectors, mask or strict RNG whose extents are multiples of
 // 32; every other configuration takes the generic phase kernel.
 
+#include "counters.cuh"
 #include "spk_internal.h"
 #include "tile_sweep.cuh"
 
@@ -35,8 +36,7 @@ __global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
   cp_async_wait<0>();
   __syncthreads();
   int changed = tile_sweep_sq4<APP, S>(j, stage);
-  unsigned int w = __reduce_add_sync(0xFFFFFFFFu, (unsigned)changed);
-  if ((threadIdx.x & 31) == 0 && w) atomicAdd(a.naccept, (unsigned long long)w);
+  block_count_add(a.naccept, (unsigned long long)changed);
 }
 
 bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny) {

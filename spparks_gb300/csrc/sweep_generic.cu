@@ -16,6 +16,7 @@
 
 #include <algorithm>
 
+#include "counters.cuh"
 #include "site_update.cuh"
 #include "spk_internal.h"
 
@@ -95,8 +96,7 @@ __global__ void __launch_bounds__(256) phase_kernel(PhaseArgs a) {
       }
     }
   }
-  unsigned int warp_sum = __reduce_add_sync(0xFFFFFFFFu, changed_count);
-  if ((threadIdx.x & 31) == 0 && warp_sum) atomicAdd(a.naccept, (unsigned long long)warp_sum);
+  block_count_add(a.naccept, changed_count);
 }
 
 template <typename S, int LAT>

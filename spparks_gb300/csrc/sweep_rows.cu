@@ -1,0 +1,236 @@
+// Row-pair sweep for sq/8n and sc/26n (no sectors): one launch per pair of
+// colours.  On these lattices colour = 4(z%2) + 2(y%2) + (x%2) + 1
+// (Lattice::id2color, src/lattice.cpp:240-276), so colours 2k-1 and 2k are
+// the even and odd x of the rows with one (y%2, z%2), and the only
+// colour-(2k-1) neighbours of a colour-2k site are its two x-neighbours in
+// the same row.  A CTA therefore sweeps whole x-rows: it stages the row and
+// its 8 (3d) or 2 (2d) neighbouring rows in shared memory, updates the even
+// sites, synchronises, then the odd sites - each thread owning one x-pair
+// whose Philox block serves both of its sites.  Rows of other parities are
+// not written during the launch, so the order equals the reference's colour
+// order (src/app_lattice.cpp:672-680).
+//
+// The distinct-value list of potts/neighonly and potts/neigh
+// (src/app_potts_neighonly.cpp:80-88) is built with a 128-bit seen-set when
+// every value is below 128, else with the pairwise scan.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "counters.cuh"
+#include "site_update.cuh"
+#include "spk_internal.h"
+
+namespace spk {
+
+// first-appearance mask of the distinct values != own among nb[] (values
+// 1..127): one test-and-set per neighbour in a 128-bit seen-set held as two
+// 64-bit words
+template <int NN>
+__device__ __forceinline__ uint32_t first_appearance_small(int own, const int (&nb)[NN]) {
+  uint64_t lo = 0, hi = 0;
+  {
+    uint64_t b = 1ull << (own & 63);
+    if (own & 64) hi = b;
+    else lo = b;
+  }
+  uint32_t first = 0;
+#pragma unroll
+  for (int j = 0; j < NN; j++) {
+    int v = nb[j];
+    uint64_t b = 1ull << (v & 63);
+    bool upper = (v & 64) != 0;
+    uint64_t cur = upper ? hi : lo;
+    first |= ((cur & b) ? 0u : 1u) << j;
+    hi |= upper ? b : 0ull;
+    lo |= upper ? 0ull : b;
+  }
+  return first;
+}
+
+template <int NN, int APP, bool SMALLQ>
+__device__ __forceinline__ int update_rows(int own, const int (&nb)[NN], uint32_t x0, uint32_t x1, int nspins,
+                                           const uint64_t *thr, int zero_t) {
+  if (APP == SPKGPU_ISING || APP == SPKGPU_POTTS) {
+    int e0;
+    return update_philox<NN, APP>(own, nb, x0, x1, nspins, thr, zero_t, &e0);
+  }
+  int e0 = count_unlike<NN>(own, nb);
+  // no unlike neighbour: no event and no draw (nevent == 0 below)
+  if (e0 == 0) return own;
+  uint32_t first = SMALLQ ? first_appearance_small<NN>(own, nb) : first_appearance<NN>(own, nb);
+  int nevent = __popc(first);
+  uint32_t iran;
+  if (APP == SPKGPU_POTTS_NEIGHONLY) {
+    if (nevent == 0) return own;
+    iran = scaled_pick((uint32_t)nevent, x0);
+    if (iran > (uint32_t)(nevent - 1)) iran = nevent - 1;
+  } else {
+    iran = scaled_pick((uint32_t)NN, x0);
+    if ((int)iran >= nevent) return own;
+  }
+  int news = pick_value<NN>(nb, __fns(first, 0, (int)iran + 1));
+  int e1 = count_unlike<NN>(news, nb);
+  if (e1 <= e0) return news;
+  if (zero_t) return own;
+  return ((uint64_t)x1 < thr[e1 - e0]) ? news : own;
+}
+
+struct RowArgs {
+  void *spin;
+  int nx, ny, nz;
+  int qy, qz;          // parity of the rows of this colour pair
+  uint32_t seed, sweep;
+  int nspins;
+  unsigned long long *naccept;
+  AcceptTable acc;
+};
+
+// rows staged: index (dz+1)*3 + (dy+1) for 3d, (dy+1) for 2d
+template <typename S, int LAT, int APP, bool SMALLQ>
+__global__ void __launch_bounds__(512) row_pair_kernel(RowArgs a) {
+  constexpr int NN = Stencil<LAT>::NN;
+  constexpr int NROWS = Stencil<LAT>::k3d ? 9 : 3;
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  S *rows = (S *)row_smem;
+  __shared__ uint64_t thr[kMaxNeigh + 1];
+  if (threadIdx.x <= kMaxNeigh) thr[threadIdx.x] = a.acc.thr[threadIdx.x];
+  const int nx = a.nx;
+  // this CTA's row
+  int rows_y = (a.ny - a.qy + 1) / 2;
+  int iy = blockIdx.x % rows_y, iz = blockIdx.x / rows_y;
+  int y = 2 * iy + a.qy;
+  int z = Stencil<LAT>::k3d ? 2 * iz + a.qz : 0;
+  S *spin = (S *)a.spin;
+  for (int r = 0; r < NROWS; r++) {
+    int dy = Stencil<LAT>::k3d ? (r % 3) - 1 : r - 1;
+    int dz = Stencil<LAT>::k3d ? (r / 3) - 1 : 0;
+    int yy = y + dy, zz = z + dz;
+    yy = yy < 0 ? yy + a.ny : (yy >= a.ny ? yy - a.ny : yy);
+    if (Stencil<LAT>::k3d) zz = zz < 0 ? zz + a.nz : (zz >= a.nz ? zz - a.nz : zz);
+    const S *src = spin + ((int64_t)zz * a.ny + yy) * nx;
+    for (int x = threadIdx.x; x < nx; x += blockDim.x) rows[r * nx + x] = src[x];
+  }
+  __syncthreads();
+  const int center = Stencil<LAT>::k3d ? 4 : 1;
+  const int64_t rowbase = ((int64_t)z * a.ny + y) * nx;
+  unsigned int changed = 0;
+  const RoundKeys rk = round_keys(a.seed, kStreamSweep);
+  // thread p owns the pair (2p, 2p+1); blockDim.x >= nx/2
+  const int p = threadIdx.x;
+  const bool active = 2 * p < nx;
+  uint32_t keep0 = 0, keep1 = 0;
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    if (active) {
+      int x = 2 * p + half;
+      uint32_t x0, x1;
+      if (half == 0) {
+        int64_t s = rowbase + 2 * p;
+        U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), a.sweep, 0u}, rk);
+        x0 = w.x;
+        x1 = w.y;
+        keep0 = w.z;
+        keep1 = w.w;
+      } else {
+        x0 = keep0;
+        x1 = keep1;
+      }
+      int nb[NN];
+#pragma unroll
+      for (int j = 0; j < NN; j++) {
+        int dx, dy, dz;
+        Stencil<LAT>::offset(j, dx, dy, dz);
+        int xn = x + dx;
+        xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
+        int r = Stencil<LAT>::k3d ? (dz + 1) * 3 + (dy + 1) : dy + 1;
+        nb[j] = rows[r * nx + xn];
+      }
+      int own = rows[center * nx + x];
+      int news = update_rows<NN, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr, a.acc.zero_t);
+      if (news != own) {
+        rows[center * nx + x] = (S)news;
+        spin[rowbase + x] = (S)news;
+        changed++;
+      }
+    }
+    __syncthreads();
+  }
+  block_count_add(a.naccept, changed);
+}
+
+bool rows_supported(int lattice, int spin_bytes, int nx, int nspins) {
+  return (lattice == SPKGPU_SQ_8N || lattice == SPKGPU_SC_26N) && nx <= 1024 && nx % 2 == 0 &&
+         (spin_bytes == 1 || spin_bytes == 2 || spin_bytes == 4) && nspins >= 1;
+}
+
+template <typename S, int LAT, int APP>
+static cudaError_t launch_rows_app(const RowArgs &a, bool smallq, cudaStream_t st) {
+  constexpr int NROWS = Stencil<LAT>::k3d ? 9 : 3;
+  int rows_y = (a.ny - a.qy + 1) / 2;
+  int rows_z = Stencil<LAT>::k3d ? (a.nz - a.qz + 1) / 2 : 1;
+  unsigned grid = (unsigned)(rows_y * rows_z);
+  size_t smem = (size_t)NROWS * a.nx * sizeof(S);
+  int threads = ((a.nx / 2 + 31) / 32) * 32;  // one x-pair per thread
+  if (smallq) {
+    auto f = row_pair_kernel<S, LAT, APP, true>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    f<<<grid, threads, smem, st>>>(a);
+  } else {
+    auto f = row_pair_kernel<S, LAT, APP, false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    f<<<grid, threads, smem, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+template <typename S, int LAT>
+static cudaError_t launch_rows_lat(int app, const RowArgs &a, bool smallq, cudaStream_t st) {
+  switch (app) {
+    case SPKGPU_ISING: return launch_rows_app<S, LAT, SPKGPU_ISING>(a, smallq, st);
+    case SPKGPU_POTTS: return launch_rows_app<S, LAT, SPKGPU_POTTS>(a, smallq, st);
+    case SPKGPU_POTTS_NEIGHONLY: return launch_rows_app<S, LAT, SPKGPU_POTTS_NEIGHONLY>(a, smallq, st);
+    case SPKGPU_POTTS_NEIGH: return launch_rows_app<S, LAT, SPKGPU_POTTS_NEIGH>(a, smallq, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename S>
+static cudaError_t launch_rows_t(int lattice, int app, const RowArgs &a, bool smallq, cudaStream_t st) {
+  if (lattice == SPKGPU_SQ_8N) return launch_rows_lat<S, SPKGPU_SQ_8N>(app, a, smallq, st);
+  return launch_rows_lat<S, SPKGPU_SC_26N>(app, a, smallq, st);
+}
+
+// one sweep: colour pairs (1,2), (3,4)[, (5,6), (7,8)] in order
+cudaError_t launch_rows_sweep(int lattice, int app, int spin_bytes, void *spin, int nx, int ny, int nz,
+                              uint32_t seed, uint32_t sweep, int nspins, unsigned long long *naccept,
+                              const AcceptTable &acc, cudaStream_t st, int *launches) {
+  bool smallq = nspins <= 127;
+  int npairs = lattice == SPKGPU_SC_26N ? 4 : 2;
+  for (int cp = 0; cp < npairs; cp++) {
+    RowArgs a;
+    a.spin = spin;
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.qy = cp & 1;
+    a.qz = (cp >> 1) & 1;
+    a.seed = seed;
+    a.sweep = sweep;
+    a.nspins = nspins;
+    a.naccept = naccept;
+    a.acc = acc;
+    cudaError_t e;
+    switch (spin_bytes) {
+      case 1: e = launch_rows_t<int8_t>(lattice, app, a, smallq, st); break;
+      case 2: e = launch_rows_t<int16_t>(lattice, app, a, smallq, st); break;
+      case 4: e = launch_rows_t<int32_t>(lattice, app, a, smallq, st); break;
+      default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    (*launches)++;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace spk

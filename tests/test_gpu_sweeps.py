@@ -70,6 +70,8 @@ def test_strict_matches_unmodified_reference(sg, ref_fixtures, k):
 
 
 RANDOM_CASES = [
+    dict(lattice="sc/26n", nx=16, ny=10, nz=6, app="potts", nspins=300, temperature=0.6),
+    dict(lattice="sq/8n", nx=34, ny=12, nz=1, app="ising", nspins=2, temperature=1.7),
     dict(lattice="sq/4n", nx=64, ny=48, nz=1, app="potts", nspins=50, temperature=0.9),
     dict(lattice="sq/8n", nx=40, ny=40, nz=1, app="potts/neighonly", nspins=30, temperature=0.4),
     dict(lattice="sc/6n", nx=16, ny=12, nz=10, app="ising", nspins=2, temperature=4.5115),
@@ -80,8 +82,11 @@ RANDOM_CASES = [
 ]
 
 
+@pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("case", RANDOM_CASES, ids=lambda c: f"{c['app']}-{c['lattice']}-{c.get('nsector', 1)}")
-def test_random_cases_match_oracle(sg, case):
+def test_random_cases_match_oracle(sg, case, variant):
+    """variant 0 takes the fastest kernel (fused tile, row-pair or packed),
+    variant 1 always the per-colour phase kernel."""
     seed = 97531
     n = case["nx"] * case["ny"] * case["nz"]
     spin = oracle.init_spins(seed, n, 1, case["nspins"])
@@ -89,7 +94,8 @@ def test_random_cases_match_oracle(sg, case):
                           case["temperature"], case.get("nsector", 1), 1, 0, seed)
     ref = spin.copy()
     na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 5)
-    lat = make_lattice(sg, case, seed=seed)
+    lat = sg.Lattice(case["lattice"], case["nx"], case["ny"], case["nz"], case["app"], case["nspins"],
+                     nsector=case.get("nsector", 1), seed=seed, variant=variant)
     lat.set_temperature(case["temperature"])
     lat.upload(spin)
     got = []
