@@ -100,6 +100,8 @@ EXPORTS = [
     "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
     "spkgpu_ensemble_get_stats", "spkgpu_ensemble_temperatures", "spkgpu_ensemble_energies",
     "spkgpu_ensemble_launch_count", "spkgpu_sweep_sq4_noalloc",
+    "spparks_open_no_mpi", "spparks_close", "spparks_file", "spparks_command", "spparks_extract", "spparks_energy",
+    "spkgpu_driver_error", "spkgpu_driver_time",
 ]
 
 _lib = None
@@ -365,3 +367,85 @@ class Ensemble:
         c = ctypes.c_int64()
         self._check(self.lib.spkgpu_ensemble_launch_count(self.h, ctypes.byref(c)))
         return c.value
+
+
+class SPPARKS:
+    """The reference's Python wrapper interface (python/spparks.py: command,
+    file, extract, energy, close) over libspkgpu.so's input-script driver.
+
+    ``extract(name, type)`` follows the reference's type codes: 0 = int
+    scalar, 1 = int vector, 3 = double scalar (``extract("site", 1)`` returns a
+    writable ctypes int pointer to the site values; writes are taken as the
+    current values by the next ``run``)."""
+
+    def __init__(self, name="", cmdargs=None):
+        self.lib = load_library()
+        self.lib.spparks_open_no_mpi.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                                 ctypes.POINTER(ctypes.c_void_p)]
+        self.lib.spparks_close.argtypes = [ctypes.c_void_p]
+        self.lib.spparks_file.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        self.lib.spparks_command.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        self.lib.spparks_command.restype = ctypes.c_char_p
+        self.lib.spparks_extract.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        self.lib.spparks_extract.restype = ctypes.c_void_p
+        self.lib.spparks_energy.argtypes = [ctypes.c_void_p]
+        self.lib.spparks_energy.restype = ctypes.c_double
+        self.lib.spkgpu_driver_error.argtypes = [ctypes.c_void_p]
+        self.lib.spkgpu_driver_error.restype = ctypes.c_char_p
+        self.lib.spkgpu_driver_time.argtypes = [ctypes.c_void_p]
+        self.lib.spkgpu_driver_time.restype = ctypes.c_double
+        args = ["spparks.py"] + list(cmdargs or [])
+        cargs = (ctypes.c_char_p * len(args))(*[a.encode() for a in args])
+        self.spk = ctypes.c_void_p()
+        self.lib.spparks_open_no_mpi(len(args), cargs, ctypes.byref(self.spk))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def close(self):
+        if getattr(self, "spk", None):
+            self.lib.spparks_close(self.spk)
+            self.spk = None
+
+    def file(self, path):
+        self.lib.spparks_file(self.spk, str(path).encode())
+
+    def command(self, cmd):
+        r = self.lib.spparks_command(self.spk, cmd.encode())
+        if r is None:
+            raise SpkGpuError(-1, self.lib.spkgpu_driver_error(self.spk).decode())
+        return r.decode()
+
+    def extract(self, name, type):
+        p = self.lib.spparks_extract(self.spk, name.encode())
+        if not p:
+            return None
+        if type == 0:
+            return ctypes.cast(p, ctypes.POINTER(ctypes.c_int))[0]
+        if type == 1:
+            return ctypes.cast(p, ctypes.POINTER(ctypes.c_int))
+        if type == 3:
+            return ctypes.cast(p, ctypes.POINTER(ctypes.c_double))[0]
+        if type == 4:
+            return ctypes.cast(p, ctypes.POINTER(ctypes.c_double))
+        return None
+
+    def sites(self) -> np.ndarray:
+        """Copy of the site values (iarray[0])."""
+        n = self.extract("nlocal", 0)
+        ptr = self.extract("site", 1)
+        return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+    def set_sites(self, values):
+        n = self.extract("nlocal", 0)
+        ptr = self.extract("site", 1)
+        np.ctypeslib.as_array(ptr, shape=(n,))[:] = np.asarray(values, dtype=np.int32)
+
+    def energy(self):
+        return self.lib.spparks_energy(self.spk)
+
+    def time(self):
+        return self.lib.spkgpu_driver_time(self.spk)

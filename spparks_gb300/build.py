@@ -28,6 +28,7 @@ SOURCES = [
     "noalloc.cu",
     "packed.cu",
     "sweep_rows.cu",
+    "driver.cpp",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

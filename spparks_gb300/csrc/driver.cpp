@@ -1,0 +1,670 @@
+// Input-script driver behind the reference's library interface
+// (src/library.h: spparks_open_no_mpi, spparks_close, spparks_file,
+// spparks_command, spparks_extract, spparks_energy; bound by python/spparks.py),
+// running the GB300 kernels through the spkgpu C ABI.
+//
+// It accepts the commands of the hot path with the reference's meaning:
+//   seed N                          Input::seed (src/input.cpp:942-951)
+//   app_style ising | potts Q | potts/neighonly Q | potts/neigh Q
+//   dimension 2|3, lattice sq/4n|sq/8n|sc/6n|sc/26n 1.0
+//   region NAME block 0 NX 0 NY (-0.5 0.5 | 0 NZ), create_box, create_sites
+//   processors PX PY PZ              Domain::set_processors
+//   set site range LO HI | set site value V   (Set::command, src/set.cpp)
+//   sweep color | color/strict [mask yes|no]   (AppLattice::set_sweep)
+//   sector yes|no|2|4|8 [nstop N | tstop T]     (AppLattice::set_sector)
+//   temperature T, solve_style tree | none, stats DT, diag_style energy
+//   run DT [upto] [pre yes|no] [post yes|no]    (App::run, src/app.cpp:86-148)
+// Output-only commands (dump, diag_style cluster, ...) are accepted and
+// ignored with a warning.  `sweep random|raster` (serial by definition) is
+// refused.  Errors are printed as "ERROR: ..." like Error::all, but the
+// process is not terminated: the command returns NULL and the message stays
+// readable through spkgpu_driver_error().
+//
+// Random numbers: the master stream is the reference's Marsaglia generator
+// (RanMars, src/random_mars.cpp) and per-use streams its Park-Miller
+// RandomPark (src/random_park.cpp), consumed in the reference's order
+// (`set site range`: one master draw; first run: two draws for ranapp, two
+// more for color/strict per-site seeds), so initial values and color/strict
+// runs equal the unmodified reference's.  `sweep color` draws Philox words
+// keyed by the `seed` value.
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/spkgpu.h"
+
+namespace {
+
+// Marsaglia RNG of RanMars (src/random_mars.cpp:43-105): the published
+// universal generator of Marsaglia, Zaman and Tsang
+struct MasterRng {
+  double u[98];
+  double c, cd, cm;
+  int i97, j97;
+  bool ready = false;
+  void init(int seed) {
+    int ij, kl, i, j, k, l, ii, jj, m;
+    while (seed > 900000000) seed -= 900000000;
+    ij = (seed - 1) / 30082;
+    kl = (seed - 1) - 30082 * ij;
+    i = (ij / 177) % 177 + 2;
+    j = ij % 177 + 2;
+    k = (kl / 169) % 178 + 1;
+    l = kl % 169;
+    for (ii = 1; ii <= 97; ii++) {
+      double s = 0.0, t = 0.5;
+      for (jj = 1; jj <= 24; jj++) {
+        m = ((i * j) % 179) * k % 179;
+        i = j;
+        j = k;
+        k = m;
+        l = (53 * l + 1) % 169;
+        if ((l * m) % 64 >= 32) s = s + t;
+        t = 0.5 * t;
+      }
+      u[ii] = s;
+    }
+    c = 362436.0 / 16777216.0;
+    cd = 7654321.0 / 16777216.0;
+    cm = 16777213.0 / 16777216.0;
+    i97 = 97;
+    j97 = 33;
+    ready = true;
+    uniform();
+  }
+  double uniform() {
+    double uni = u[i97] - u[j97];
+    if (uni < 0.0) uni += 1.0;
+    u[i97] = uni;
+    if (--i97 == 0) i97 = 97;
+    if (--j97 == 0) j97 = 97;
+    c -= cd;
+    if (c < 0.0) c += cm;
+    uni -= c;
+    if (uni < 0.0) uni += 1.0;
+    return uni;
+  }
+};
+
+// Park-Miller minimal standard (Park & Miller 1988) with Schrage's
+// factorisation, the RandomPark recurrence (src/random_park.cpp:79-86)
+struct Park {
+  int seed = 1;
+  static int from_double(double r) {
+    int s = (int)(r * 2147483647);
+    return s == 0 ? 1 : s;
+  }
+  static int reset(double r, long long offset, int warmup) {
+    Park p;
+    p.seed = (int)fmod(r * 2147483647 + (double)offset, 2147483647);
+    if (p.seed < 0) p.seed = -p.seed;
+    if (p.seed == 0) p.seed = 1;
+    for (int i = 0; i < warmup; i++) p.uniform();
+    return p.seed;
+  }
+  double uniform() {
+    int k = seed / 127773;
+    seed = 16807 * (seed - k * 127773) - 2836 * k;
+    if (seed < 0) seed += 2147483647;
+    return (1.0 / 2147483647) * seed;
+  }
+  int irandom(int n) {
+    int i = (int)(uniform() * n) + 1;
+    return i > n ? n : i;
+  }
+};
+
+enum { SWEEP_NONE = 0, SWEEP_COLOR = 1, SWEEP_STRICT = 2 };
+
+struct Driver {
+  FILE *screen = stdout;
+  FILE *logfile = nullptr;
+  std::string error;
+  MasterRng master;
+  int seed = 0;
+  // app
+  std::string app;
+  int app_id = -1, nspins = 0;
+  int dimension = 3;
+  int lattice = -1;
+  double latconst = 1.0;
+  int nx = 0, ny = 0, nz = 0;
+  bool have_region = false, box = false, sites = false;
+  int procs[3] = {1, 1, 1};
+  std::vector<int32_t> site;       // host copy of iarray[0]
+  bool host_valid = false;         // host copy is current (or authoritative)
+  bool device_valid = false;       // device copy is current
+  int sweepflag = SWEEP_NONE;
+  bool mask = false;
+  int nsector_user = 0, sectorflag = 0;
+  double nstop = 1.0, tstop = 0.0;
+  double temperature = 0.0;
+  bool tree = false;
+  double stats_delta = 0.0;
+  bool diag_energy = false;
+  // run state
+  double time = 0.0;
+  int64_t nsweeps = 0, naccept = 0, nattempt = 0;
+  bool first_run = true;
+  spkgpu_lattice *h = nullptr;
+  int h_key[13] = {0};
+  bool kmc_ready = false;
+  std::vector<int32_t> siteseeds;
+  bool seeds_on_device = false;
+  std::string extract_name;
+  int64_t nglobal_store = 0;
+  int nlocal_store = 0;
+  double box_store[6] = {0, 0, 0, 0, 0, 0};
+
+  ~Driver() {
+    if (h) spkgpu_destroy(h);
+    if (logfile) fclose(logfile);
+  }
+
+  void print(const char *fmt, ...) {
+    char buf[4096];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (screen) fputs(buf, screen);
+    if (logfile) fputs(buf, logfile);
+  }
+
+  bool fail(const std::string &m) {
+    error = m;
+    print("ERROR: %s\n", m.c_str());
+    return false;
+  }
+
+  int64_t n() const { return (int64_t)nx * ny * nz; }
+  int maxneigh() const {
+    static const int mn[4] = {4, 8, 6, 26};
+    return lattice >= 0 ? mn[lattice] : 0;
+  }
+  double dt_sweep() const {
+    if (app_id == SPKGPU_ISING) return 1.0 / 2.0;
+    if (app_id == SPKGPU_POTTS) return 1.0 / nspins;
+    return 1.0 / maxneigh();
+  }
+  int nsector() const {
+    if (!sectorflag) return 1;
+    if (nsector_user) return nsector_user;
+    return dimension == 2 ? 4 : 8;
+  }
+  // passes over each set per sweep (src/app_lattice.cpp:398-407)
+  int nloop() const {
+    if (sweepflag == SWEEP_NONE) return 1;
+    if (tstop > 0.0) return (int)(tstop / dt_sweep());
+    return (int)nstop;
+  }
+
+  bool command(std::vector<std::string> &w);
+  bool run(std::vector<std::string> &w);
+  bool ensure_handle();
+  bool sync_to_host();
+  void stats_line(double cpu);
+};
+
+double wall() {
+  struct timeval tv;
+  gettimeofday(&tv, nullptr);
+  return tv.tv_sec + 1e-6 * tv.tv_usec;
+}
+
+bool parse_int(const std::string &s, int *out) {
+  char *e = nullptr;
+  long v = strtol(s.c_str(), &e, 10);
+  if (!e || *e) return false;
+  *out = (int)v;
+  return true;
+}
+
+bool parse_double(const std::string &s, double *out) {
+  char *e = nullptr;
+  double v = strtod(s.c_str(), &e);
+  if (!e || *e) return false;
+  *out = v;
+  return true;
+}
+
+bool Driver::sync_to_host() {
+  if (host_valid) return true;
+  if (!h || !device_valid) return true;
+  site.resize(n());
+  if (spkgpu_download_spins(h, site.data(), n()) != 0) return fail(spkgpu_last_error(h));
+  host_valid = true;
+  return true;
+}
+
+bool Driver::ensure_handle() {
+  int key[13] = {lattice, nx, ny, nz, app_id, nspins, nsector(), procs[0], procs[1], procs[2],
+                 sweepflag == SWEEP_STRICT ? 1 : 0, mask ? 1 : 0, nloop()};
+  if (h && memcmp(key, h_key, sizeof(key)) == 0) return true;
+  if (h) {
+    if (!sync_to_host()) return false;
+    spkgpu_destroy(h);
+    h = nullptr;
+    device_valid = false;
+    seeds_on_device = false;
+    kmc_ready = false;
+  }
+  spkgpu_desc d;
+  memset(&d, 0, sizeof(d));
+  d.lattice = lattice;
+  d.nx = nx;
+  d.ny = ny;
+  d.nz = nz;
+  d.app = app_id;
+  d.nspins = nspins;
+  d.spin_bytes = 0;
+  d.nsector = nsector();
+  d.nloop = nloop() < 1 ? 1 : nloop();
+  d.procs[0] = procs[0];
+  d.procs[1] = procs[1];
+  d.procs[2] = procs[2];
+  d.rng = sweepflag == SWEEP_STRICT ? SPKGPU_RNG_STRICT : SPKGPU_RNG_PHILOX;
+  d.mask = mask ? 1 : 0;
+  d.seed = (uint32_t)seed;
+  d.device = 0;
+  d.variant = 0;
+  int rc = spkgpu_create(&d, &h);
+  if (rc != 0) return fail("the GPU path cannot run this configuration (spkgpu_create returned " +
+                           std::to_string(rc) + ")");
+  memcpy(h_key, key, sizeof(key));
+  return true;
+}
+
+void Driver::stats_line(double cpu) {
+  char line[256];
+  int off = snprintf(line, sizeof(line), "%10g %10lld %10lld %10lld %10.3g", time, (long long)naccept,
+                     (long long)(tree ? 0 : nattempt - naccept), (long long)nsweeps, cpu);
+  if (diag_energy && h) {
+    double e = 0.0;
+    if (spkgpu_energy(h, &e) == 0) snprintf(line + off, sizeof(line) - off, " %10g", e);
+  }
+  print("%s\n", line);
+}
+
+bool Driver::run(std::vector<std::string> &w) {
+  if (app_id < 0) return fail("Run command before app_style set");
+  if (!box) return fail("Cannot run application until simulation box is defined");
+  if (!sites) return fail("Cannot run application until sites exist");
+  if (w.size() < 2) return fail("Illegal run command");
+  double delta;
+  if (!parse_double(w[1], &delta)) return fail("Illegal run command");
+  double stoptime = time + delta;
+  if (stoptime < time) return fail("Illegal run command");
+  bool upto = false;
+  for (size_t k = 2; k < w.size(); k++) {
+    if (w[k] == "upto") upto = true;
+    else if ((w[k] == "pre" || w[k] == "post") && k + 1 < w.size()) k++;
+    else return fail("Illegal run command");
+  }
+  if (upto) stoptime -= time;
+  if (!tree && sweepflag == SWEEP_NONE) return fail("App needs a KMC or rejection KMC solver");
+  if (tree && sweepflag != SWEEP_NONE) return fail("App cannot use both a KMC and rejection KMC solver");
+  if (sectorflag && sweepflag == SWEEP_STRICT) return fail("Cannot use color/strict rejection KMC with sectors");
+  if (tree && !sectorflag) return fail("the GPU path runs tree KMC with sectors (sector yes)");
+  if (host_valid)
+    for (int32_t v : site)
+      if (v < 1 || v > nspins) return fail("One or more sites have invalid values");
+  if (!ensure_handle()) return false;
+  // first run: ranapp (two master draws), then the color/strict seeds
+  // (src/app_lattice.cpp:274-295)
+  if (first_run) {
+    if (!master.ready) return fail("Seed command has not been used");
+    master.uniform();
+    master.uniform();
+    if (sweepflag == SWEEP_STRICT) {
+      master.uniform();
+      double rs = master.uniform();
+      siteseeds.resize(n());
+      for (int64_t i = 0; i < n(); i++) siteseeds[i] = Park::reset(rs, i + 1, 100);
+    }
+  }
+  if (spkgpu_set_temperature(h, temperature) != 0) return fail(spkgpu_last_error(h));
+  if (!device_valid) {
+    if (spkgpu_upload_spins(h, site.data(), n()) != 0) return fail(spkgpu_last_error(h));
+    device_valid = true;
+  }
+  if (sweepflag == SWEEP_STRICT && !seeds_on_device) {
+    if (spkgpu_upload_siteseeds(h, siteseeds.data(), n()) != 0) return fail(spkgpu_last_error(h));
+    seeds_on_device = true;
+  }
+  host_valid = false;
+  first_run = false;
+  print("Setting up run ...\n");
+  print("%10s %10s %10s %10s %10s%s\n", "Time", "Naccept", "Nreject", "Nsweeps", "CPU",
+        diag_energy ? "     Energy" : "");
+  double t0 = wall();
+  stats_line(0.0);
+  double nextoutput = stats_delta > 0.0 ? time + stats_delta : stoptime;
+  if (tree) {
+    spkgpu_kmc_stats ks;
+    // one solver state per handle: consecutive runs continue its event
+    // counters, as the reference reuses its solvers (src/app_lattice.cpp:205-211)
+    if (!kmc_ready) {
+      if (spkgpu_kmc_setup(h, tstop > 0.0 ? 0 : 1, nstop, tstop, 1) != 0) return fail(spkgpu_last_error(h));
+      kmc_ready = true;
+    }
+    if (stoptime > time) {
+      if (spkgpu_kmc_run(h, &time, stoptime, &ks) != 0) return fail(spkgpu_last_error(h));
+      naccept = ks.naccept;
+      nsweeps = ks.npass;
+    }
+    stats_line(wall() - t0);
+  } else {
+    // rejection KMC: dt_rkmc = nloop * dt_sweep per pass over all sets
+    // (src/app_lattice.cpp:398-420)
+    if (nloop() < 1) return fail("Choice of sector stop led to no rKMC events");
+    double dt_rkmc = nloop() * dt_sweep();
+    dt_rkmc = fmin(dt_rkmc, stoptime - time);
+    bool done = !(stoptime > time);
+    while (!done) {
+      if (spkgpu_sweep(h, 1) != 0) return fail(spkgpu_last_error(h));
+      nsweeps++;
+      time += dt_rkmc;
+      if (time >= stoptime) done = true;
+      if (done || time >= nextoutput) {
+        spkgpu_stats st;
+        if (spkgpu_get_stats(h, &st) != 0) return fail(spkgpu_last_error(h));
+        naccept = st.naccept;
+        nattempt = st.nattempt;
+        stats_line(wall() - t0);
+        if (stats_delta > 0.0)
+          while (nextoutput <= time) nextoutput += stats_delta;
+      }
+    }
+  }
+  print("Loop time of %g on 1 procs\n\n", wall() - t0);
+  return true;
+}
+
+bool Driver::command(std::vector<std::string> &w) {
+  const std::string &c = w[0];
+  auto need = [&](size_t k) { return w.size() >= k; };
+  if (c == "seed") {
+    int s;
+    if (w.size() != 2 || !parse_int(w[1], &s) || s <= 0) return fail("Illegal seed command");
+    seed = s;
+    master.init(s);
+  } else if (c == "app_style") {
+    if (box) return fail("App_style command after simulation box is defined");
+    if (!need(2)) return fail("Illegal app_style command");
+    app = w[1];
+    if (app == "ising") {
+      if (w.size() != 2) return fail("Illegal app_style command");
+      app_id = SPKGPU_ISING;
+      nspins = 2;
+    } else if (app == "potts" || app == "potts/neighonly" || app == "potts/neigh") {
+      if (w.size() != 3 || !parse_int(w[2], &nspins) || nspins <= 0) return fail("Illegal app_style command");
+      app_id = app == "potts" ? SPKGPU_POTTS : (app == "potts/neighonly" ? SPKGPU_POTTS_NEIGHONLY : SPKGPU_POTTS_NEIGH);
+    } else {
+      return fail("app_style " + app + " is not on the GPU path (ising, potts, potts/neighonly, potts/neigh)");
+    }
+  } else if (c == "dimension") {
+    if (w.size() != 2 || !parse_int(w[1], &dimension) || (dimension != 2 && dimension != 3))
+      return fail("Illegal dimension command");
+  } else if (c == "lattice") {
+    if (w.size() != 3 || !parse_double(w[2], &latconst)) return fail("Illegal lattice command");
+    static const char *names[4] = {"sq/4n", "sq/8n", "sc/6n", "sc/26n"};
+    lattice = -1;
+    for (int k = 0; k < 4; k++)
+      if (w[1] == names[k]) lattice = k;
+    if (lattice < 0) return fail("lattice " + w[1] + " is not on the GPU path (sq/4n, sq/8n, sc/6n, sc/26n)");
+    if (latconst != 1.0) return fail("the GPU path takes lattice constant 1.0");
+    if ((lattice <= 1) != (dimension == 2)) return fail("Lattice style does not match dimension");
+  } else if (c == "region") {
+    if (w.size() != 9 || w[2] != "block") return fail("the GPU path takes one region: NAME block 0 NX 0 NY ZLO ZHI");
+    double b[6];
+    for (int k = 0; k < 6; k++)
+      if (!parse_double(w[3 + k], &b[k])) return fail("Illegal region command");
+    if (b[0] != 0.0 || b[2] != 0.0 || b[1] != floor(b[1]) || b[3] != floor(b[3]))
+      return fail("region bounds must be 0 .. N in lattice units");
+    nx = (int)b[1];
+    ny = (int)b[3];
+    if (dimension == 2) {
+      if (b[4] != -0.5 || b[5] != 0.5) return fail("2d regions span z -0.5 0.5");
+      nz = 1;
+    } else {
+      if (b[4] != 0.0 || b[5] != floor(b[5])) return fail("region bounds must be 0 .. N in lattice units");
+      nz = (int)b[5];
+    }
+    for (int k = 0; k < 6; k++) box_store[k] = b[k];
+    have_region = true;
+  } else if (c == "create_box") {
+    if (!have_region || app_id < 0 || lattice < 0) return fail("Create_box command before region/app/lattice");
+    box = true;
+  } else if (c == "create_sites") {
+    if (!box) return fail("Create_sites command before simulation box is defined");
+    sites = true;
+    site.assign(n(), 0);
+    host_valid = true;
+    device_valid = false;
+    print("Creating sites ...\n  %lld sites\n", (long long)n());
+  } else if (c == "processors") {
+    if (w.size() != 4) return fail("Illegal processors command");
+    for (int k = 0; k < 3; k++)
+      if (!parse_int(w[1 + k], &procs[k]) || procs[k] < 1) return fail("Illegal processors command");
+  } else if (c == "set") {
+    if (!sites) return fail("Set command before sites exist");
+    if (w.size() < 3 || w[1] != "site") return fail("the GPU driver supports `set site range|value`");
+    if (!sync_to_host()) return false;
+    if (w[2] == "value" && w.size() == 4) {
+      int v;
+      if (!parse_int(w[3], &v)) return fail("Illegal set command");
+      for (auto &x : site) x = v;
+    } else if (w[2] == "range" && w.size() == 5) {
+      int lo, hi;
+      if (!parse_int(w[3], &lo) || !parse_int(w[4], &hi)) return fail("Illegal set command");
+      if (!master.ready) return fail("Seed command has not been used");
+      // loop option (the default): one stream over all site IDs in order
+      Park p;
+      p.seed = Park::from_double(master.uniform());
+      for (auto &x : site) x = p.irandom(hi - lo + 1) - 1 + lo;
+    } else {
+      return fail("the GPU driver supports `set site range LO HI` and `set site value V`");
+    }
+    host_valid = true;
+    device_valid = false;
+    print("  %lld settings made for site\n", (long long)n());
+  } else if (c == "sweep") {
+    if (!need(2)) return fail("Illegal sweep command");
+    if (w[1] == "color") sweepflag = SWEEP_COLOR;
+    else if (w[1] == "color/strict") sweepflag = SWEEP_STRICT;
+    else if (w[1] == "none") sweepflag = SWEEP_NONE;
+    else if (w[1] == "random" || w[1] == "raster")
+      return fail("sweep " + w[1] + " is a serial site order; the GPU path runs sweep color and color/strict");
+    else return fail("Illegal sweep command");
+    mask = false;
+    for (size_t k = 2; k < w.size(); k += 2) {
+      if (w[k] != "mask" || k + 1 >= w.size()) return fail("Illegal sweep command");
+      if (w[k + 1] == "yes") mask = true;
+      else if (w[k + 1] == "no") mask = false;
+      else return fail("Illegal sweep command");
+    }
+  } else if (c == "sector") {
+    if (!need(2)) return fail("Illegal sector command");
+    nsector_user = 0;
+    if (w[1] == "yes") sectorflag = 1;
+    else if (w[1] == "no") sectorflag = 0;
+    else {
+      sectorflag = 1;
+      if (!parse_int(w[1], &nsector_user) || (nsector_user != 2 && nsector_user != 4 && nsector_user != 8))
+        return fail("Illegal sector command");
+    }
+    nstop = 1.0;
+    tstop = 0.0;
+    for (size_t k = 2; k < w.size(); k += 2) {
+      double v;
+      if (k + 1 >= w.size() || !parse_double(w[k + 1], &v) || v <= 0.0) return fail("Illegal sector command");
+      if (w[k] == "nstop") {
+        nstop = v;
+        tstop = 0.0;
+      } else if (w[k] == "tstop") {
+        tstop = v;
+        nstop = 0.0;
+      } else {
+        return fail("Illegal sector command");
+      }
+    }
+  } else if (c == "temperature") {
+    if (w.size() != 2 || !parse_double(w[1], &temperature)) return fail("Illegal temperature command");
+  } else if (c == "solve_style") {
+    if (app_id < 0) return fail("Solve_style command before app_style set");
+    if (!need(2)) return fail("Illegal solve_style command");
+    if (w[1] == "tree") {
+      tree = true;
+      // SolveTree's own RandomPark (src/solve_tree.cpp:25-27): two master draws
+      if (master.ready) {
+        master.uniform();
+        master.uniform();
+      }
+    } else if (w[1] == "none") {
+      tree = false;
+    } else {
+      return fail("solve_style " + w[1] + " is not on the GPU path (tree)");
+    }
+  } else if (c == "stats") {
+    if (!need(2) || !parse_double(w[1], &stats_delta)) return fail("Illegal stats command");
+  } else if (c == "diag_style") {
+    if (need(2) && w[1] == "energy") diag_energy = true;
+    else print("WARNING: diag_style %s is ignored by the GPU driver\n", need(2) ? w[1].c_str() : "");
+  } else if (c == "run") {
+    return run(w);
+  } else if (c == "dump" || c == "undump" || c == "dump_modify" || c == "echo" || c == "log" ||
+             c == "diag_style" || c == "reset_time" || c == "shell") {
+    print("WARNING: %s is ignored by the GPU driver\n", c.c_str());
+  } else {
+    return fail("Unknown command: " + c);
+  }
+  return true;
+}
+
+std::vector<std::string> split_words(const char *line) {
+  std::vector<std::string> w;
+  std::string cur;
+  for (const char *p = line; *p; p++) {
+    if (*p == '#') break;
+    if (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r') {
+      if (!cur.empty()) w.push_back(cur), cur.clear();
+    } else {
+      cur += *p;
+    }
+  }
+  if (!cur.empty()) w.push_back(cur);
+  return w;
+}
+
+}  // namespace
+
+extern "C" {
+
+void spparks_open_no_mpi(int argc, char **argv, void **ptr) {
+  Driver *d = new Driver();
+  for (int k = 1; k < argc; k++) {
+    if (!strcmp(argv[k], "-screen") && k + 1 < argc) {
+      k++;
+      if (!strcmp(argv[k], "none")) d->screen = nullptr;
+      else d->screen = fopen(argv[k], "w");
+    } else if (!strcmp(argv[k], "-log") && k + 1 < argc) {
+      k++;
+      if (strcmp(argv[k], "none")) d->logfile = fopen(argv[k], "w");
+    }
+  }
+  d->print("SPPARKS (GB300 spkgpu driver)\n");
+  *ptr = d;
+}
+
+void spparks_close(void *ptr) { delete (Driver *)ptr; }
+
+char *spparks_command(void *ptr, char *str) {
+  Driver *d = (Driver *)ptr;
+  if (!d || !str) return nullptr;
+  std::vector<std::string> w = split_words(str);
+  if (w.empty()) return str;
+  d->error.clear();
+  if (!d->command(w)) return nullptr;
+  return str;
+}
+
+void spparks_file(void *ptr, char *path) {
+  Driver *d = (Driver *)ptr;
+  FILE *fp = fopen(path, "r");
+  if (!fp) {
+    d->fail(std::string("Cannot open input script ") + path);
+    return;
+  }
+  char line[4096];
+  while (fgets(line, sizeof(line), fp)) {
+    d->print("%s", line);
+    std::vector<std::string> w = split_words(line);
+    if (w.empty()) continue;
+    if (!d->command(w)) break;
+  }
+  fclose(fp);
+}
+
+// names of src/app.cpp:163-196 that the GPU driver keeps
+void *spparks_extract(void *ptr, char *name) {
+  Driver *d = (Driver *)ptr;
+  if (!d || !name) return nullptr;
+  std::string n = name;
+  if (n == "site" || n == "iarray1") {
+    if (!d->sites || !d->sync_to_host()) return nullptr;
+    // the caller may write into it: it becomes the authoritative copy
+    d->device_valid = false;
+    return d->site.data();
+  }
+  if (n == "dimension") return &d->dimension;
+  if (n == "nglobal") {
+    d->nglobal_store = d->n();
+    return &d->nglobal_store;
+  }
+  if (n == "nlocal") {
+    d->nlocal_store = (int)d->n();
+    return &d->nlocal_store;
+  }
+  if (n == "boxxlo") return &d->box_store[0];
+  if (n == "boxxhi") return &d->box_store[1];
+  if (n == "boxylo") return &d->box_store[2];
+  if (n == "boxyhi") return &d->box_store[3];
+  if (n == "boxzlo") return &d->box_store[4];
+  if (n == "boxzhi") return &d->box_store[5];
+  return nullptr;
+}
+
+double spparks_energy(void *ptr) {
+  Driver *d = (Driver *)ptr;
+  if (!d || !d->sites) return 0.0;
+  if (d->h && d->device_valid) {
+    double e = 0.0;
+    if (spkgpu_energy(d->h, &e) == 0) return e;
+  }
+  if (!d->ensure_handle()) return 0.0;
+  if (spkgpu_upload_spins(d->h, d->site.data(), d->n()) != 0) return 0.0;
+  d->device_valid = true;
+  double e = 0.0;
+  spkgpu_energy(d->h, &e);
+  return e;
+}
+
+const char *spkgpu_driver_error(void *ptr) {
+  Driver *d = (Driver *)ptr;
+  return d ? d->error.c_str() : "null handle";
+}
+
+double spkgpu_driver_time(void *ptr) {
+  Driver *d = (Driver *)ptr;
+  return d ? d->time : 0.0;
+}
+
+}  // extern "C"

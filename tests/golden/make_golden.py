@@ -166,6 +166,47 @@ STRICT_CASES = [
 ]
 
 
+LOG_CASES = [
+    dict(name="log_strict_ising_sq4n_50", lines=[
+        "seed 56789", "app_style ising", "dimension 2", "lattice sq/4n 1.0", "region box block 0 50 0 50 -0.5 0.5",
+        "create_box box", "create_sites box", "set site range 1 2", "sweep color/strict", "diag_style energy",
+        "temperature 2.269", "stats 5.0", "run 50.0"]),
+    dict(name="log_strict_neighonly_sc26n_12", lines=[
+        "seed 4242", "app_style potts/neighonly 100", "dimension 3", "lattice sc/26n 1.0",
+        "region box block 0 12 0 12 0 12", "create_box box", "create_sites box", "set site range 1 100",
+        "sweep color/strict", "diag_style energy", "temperature 0.5", "stats 0.2", "run 1.0"]),
+    dict(name="log_strict_potts_sq8n_20_two_runs", lines=[
+        "seed 777", "app_style potts 8", "dimension 2", "lattice sq/8n 1.0", "region box block 0 20 0 20 -0.5 0.5",
+        "create_box box", "create_sites box", "set site range 1 8", "sweep color/strict", "diag_style energy",
+        "temperature 0.9", "stats 0.5", "run 2.0", "temperature 0.3", "run 1.0"]),
+]
+
+
+def spk_serial_stats(binary, lines):
+    """Stats rows (Time Naccept Nreject Nsweeps Energy) printed by the reference."""
+    with tempfile.TemporaryDirectory(dir=str(ROOT / "oracle" / "_ref")) as d:
+        inp = Path(d) / "in.case"
+        inp.write_text("\n".join(lines) + "\n")
+        subprocess.run([str(binary), "-in", "in.case", "-screen", "none", "-log", "log.case"], cwd=d, check=True,
+                       capture_output=True)
+        text = (Path(d) / "log.case").read_text().splitlines()
+    rows, grab = [], False
+    for line in text:
+        p = line.split()
+        if p[:4] == ["Time", "Naccept", "Nreject", "Nsweeps"]:
+            grab = True
+            continue
+        if grab:
+            if len(p) == 6:
+                try:
+                    rows.append([float(p[0]), int(p[1]), int(p[2]), int(p[3]), float(p[5])])
+                    continue
+                except ValueError:
+                    pass
+            grab = False
+    return rows
+
+
 def example_log_rows(path):
     rows = []
     lines = Path(path).read_text().splitlines()
@@ -208,6 +249,12 @@ def main():
         fixtures["strict"].append({"case": case, "script": lines, **res})
         print("strict case", case["name"], [res["snaps"][f"run{k}"]["hash"] for k in range(case["nruns"])])
 
+    serial = ROOT / "oracle" / "_ref" / "spk_serial"
+    fixtures["logs"] = []
+    for case in LOG_CASES:
+        rows = spk_serial_stats(serial, case["lines"])
+        fixtures["logs"].append({"case": case, "rows": rows})
+        print("log case", case["name"], len(rows), "rows")
     (HERE / "reference_philox.json").write_text(json.dumps(fixtures, indent=1))
     logs = {
         "ising": {"script": (Path(args.ref) / "examples/ising/in.ising").read_text().splitlines(),

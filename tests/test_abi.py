@@ -18,7 +18,7 @@ def declared_symbols():
     for h in (ROOT / "include").glob("*.h"):
         text = h.read_text()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(spk\w+)\s*\(", text, flags=re.M):
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b((?:spkgpu|spparks)_\w+)\s*\(", text, flags=re.M):
             names.add(m.group(1))
     return sorted(names)
 
