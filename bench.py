@@ -347,6 +347,48 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def kernel_case(name):
+    """Small fixed workloads that launch one hot kernel each, for profilers
+    (the commands in profiles/*.md); prints a one-line status."""
+    import spparks_gb300 as sg
+
+    if name == "ensemble":  # 20 replicas, 5.6e6 sites: two launches of 10 sweeps + exchange
+        L = [1024, 512, 256, 128, 64] * 4
+        T = list(np.linspace(1.5, 3.5, len(L)))
+        rng = np.random.default_rng(3)
+        ens = sg.Ensemble(L, T, "ising", 2, seed=3, exchange_every=10)
+        ens.upload(rng.integers(1, 3, sum(l * l for l in L)).astype(np.int32))
+        ens.run(10)
+        ens.run(10)
+        print("ensemble", ens.stats())
+    elif name == "fused":  # 1024^2 int8 Ising, fused tile sweeps
+        lat = sg.Lattice("sq/4n", 1024, 1024, 1, "ising", 2, spin_bytes=1, seed=5)
+        lat.set_temperature(2.269)
+        lat.init_spins(1, 2)
+        lat.sweep(5)
+        print("fused", lat.stats())
+    elif name == "rows":  # potts/neighonly Q=100 sc/26n 256x256x128 int16, row-pair sweeps
+        lat = sg.Lattice("sc/26n", 256, 256, 128, "potts/neighonly", 100, spin_bytes=2, seed=5)
+        lat.set_temperature(0.5)
+        lat.init_spins(1, 100)
+        lat.sweep(2)
+        print("rows", lat.stats())
+    elif name == "packed":  # bit-packed Ising sc/6n 512^3
+        lat = sg.Lattice("sc/6n", 512, 512, 512, "ising", 2, spin_bytes=-1, seed=5)
+        lat.set_temperature(4.5115)
+        lat.init_spins(1, 2)
+        lat.sweep(2)
+        print("packed", lat.stats())
+    elif name == "kmc":  # tree KMC Potts Q=50 sq/8n 1024^2, 32x32 processor grid, 4 sectors
+        lat = sg.Lattice("sq/8n", 1024, 1024, 1, "potts", 50, spin_bytes=4, nsector=4, procs=(32, 32, 1), seed=5)
+        lat.set_temperature(1.0)
+        lat.init_spins(1, 50)
+        lat.kmc_setup(fp64=True)
+        print("kmc", lat.kmc_run(0.0, 0.3))
+    else:
+        raise SystemExit(f"unknown kernel case {name}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,7 +396,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--kernel-case", choices=["ensemble", "fused", "rows", "packed", "kmc"],
+                    help="run one small profiling workload instead of the benchmark")
     args = ap.parse_args()
+    if args.kernel_case:
+        kernel_case(args.kernel_case)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
