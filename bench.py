@@ -156,42 +156,51 @@ def _cpu_worker(args):
     return done, time.perf_counter() - t0
 
 
-def cpu_rate(sample_replicas=24, sweeps=4, procs=1):
-    """Site-updates/s of the oracle's colour sweep on a sample of replicas."""
-    import multiprocessing as mp
-
+def cpu_rate(sample_replicas=24, sweeps=4, procs=1, pool=None, offset=0):
+    """Site-updates/s of the oracle's colour sweep on a sample of replicas
+    (wall time of the sample; `pool` is a persistent spawn pool of `procs`)."""
     L, T = ensemble_config()
-    rng = np.random.default_rng(7)
+    rng = np.random.default_rng(7 + offset)
     pick = rng.choice(len(L), size=min(sample_replicas, len(L)), replace=False)
-    reps = [(int(r), int(L[r]), float(T[r])) for r in pick]
-    chunks = [reps[i::procs] for i in range(procs)]
+    reps = sorted([(int(r), int(L[r]), float(T[r])) for r in pick], key=lambda x: -x[1])
+    # longest-processing-time assignment: equal site counts per process
+    chunks, load = [[] for _ in range(procs)], [0] * procs
+    for rep in reps:
+        k = load.index(min(load))
+        chunks[k].append(rep)
+        load[k] += rep[1] ** 2
     t0 = time.perf_counter()
-    if procs == 1:
+    if pool is None:
         results = [_cpu_worker((chunks[0], sweeps, SEED))]
     else:
-        with mp.get_context("spawn").Pool(procs) as pool:
-            results = pool.map(_cpu_worker, [(c, sweeps, SEED) for c in chunks])
+        results = pool.map(_cpu_worker, [(c, sweeps, SEED) for c in chunks])
     wall = time.perf_counter() - t0
     updates = sum(r[0] for r in results)
     return updates / wall, updates, wall
 
 
 def run_reference(args):
+    """The reference's CPU colour sweep (the oracle port: the reference's x86
+    build cannot run on the GPU host) on every host core: one spawned process
+    per core, each step 4 replicas per process (equal site counts) x 4 sweeps."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    import multiprocessing as mp
+
     import oracle
 
     oracle.build()
     procs = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_rate(sample_replicas=procs, sweeps=1, procs=procs)
-    rates, times, ups = [], [], 0
-    for _ in range(args.steps):
-        r, u, w = cpu_rate(sample_replicas=2 * procs, sweeps=2, procs=procs)
-        rates.append(r)
-        times.append(w)
-        ups += u
+    sweeps = 4
+    with mp.get_context("spawn").Pool(procs) as pool:
+        for w in range(args.warmup):
+            cpu_rate(sample_replicas=procs, sweeps=1, procs=procs, pool=pool, offset=1000 + w)
+        times, ups = [], 0
+        for k in range(args.steps):
+            r, u, w = cpu_rate(sample_replicas=4 * procs, sweeps=sweeps, procs=procs, pool=pool, offset=k)
+            times.append(w)
+            ups += u
     value = ups / sum(times)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -199,10 +208,10 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "impl": "reference",
         "config": {"workload": "batched 2D Ising ensemble, 512 sq/4n replicas L in [64,1024], kT in [1.5,3.5], "
-                               "exchange every 10 sweeps", "step": "2 sweeps of a random sample of replicas",
+                               "exchange every 10 sweeps", "step": f"{sweeps} sweeps of {4 * procs} random replicas, equal sites per core",
                    "threads": procs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": f"{2 * procs} replicas x 2 sweeps per step, oracle C restatement of "
+                         "sample": f"{4 * procs} replicas x {sweeps} sweeps per step, oracle C restatement of "
                                    "AppIsing::site_event_rejection + colour sweep, one process per core"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -211,6 +220,22 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------
 # GPU arm
+
+
+def max_over_ranks(value, dist, device="cpu"):
+    """The timed region's length on the slowest rank (the job's time)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, job_ms):
+    """Whole-job throughput: units all ranks processed / the job's time."""
+    return units_per_rank * world / (job_ms * 1e-3)
 
 
 def dist_setup(ngpus):
@@ -267,13 +292,9 @@ def run_ours(args):
     clk = clocks.stop()
     launches = ens.launch_count() - launches0
     st = ens.stats()
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), dist, f"cuda:{device}")
     updates_rank = nsites * SWEEPS_PER_STEP * args.steps
-    value = updates_rank * world / (total_ms * 1e-3)
+    value = whole_job_rate(updates_rank, world, total_ms)
     ms_step = total_ms / args.steps
 
     # end to end through the C ABI with pinned host buffers
@@ -288,8 +309,8 @@ def run_ours(args):
         ens.run(SWEEPS_PER_STEP)
         ens.download(eout)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = nsites * SWEEPS_PER_STEP * e2e_steps * world / e2e_s
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3, dist, f"cuda:{device}")
+    e2e_value = whole_job_rate(nsites * SWEEPS_PER_STEP * e2e_steps, world, e2e_ms)
 
     # plain GPU sweep: the same replicas one by one with the per-colour phase
     # kernel (a sample of replicas, 10 sweeps each, extrapolated by sites)
@@ -318,9 +339,9 @@ def run_ours(args):
         import oracle
 
         oracle.build()
-        r1, u1, w1 = cpu_rate(sample_replicas=6, sweeps=4, procs=1)
+        r1, u1, w1 = cpu_rate(sample_replicas=48, sweeps=10, procs=1)
         cpu = {"value": r1, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"6 random replicas x 4 sweeps ({u1:.3g} site-updates, {w1:.1f} s), oracle C "
+               "sample": f"48 random replicas x 10 sweeps ({u1:.3g} site-updates, {w1:.1f} s), oracle C "
                          "restatement of the reference colour sweep, 1 thread"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
