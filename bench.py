@@ -373,8 +373,8 @@ def kernel_case(name):
     (the commands in profiles/*.md); prints a one-line status."""
     import spparks_gb300 as sg
 
-    if name == "ensemble":  # 20 replicas, 5.6e6 sites: two launches of 10 sweeps + exchange
-        L = [1024, 512, 256, 128, 64] * 4
+    if name == "ensemble":  # 160 uneven replicas, 1.06e8 sites (2 x 106 MB > L2): two launches of 10 sweeps
+        L = [1024, 768, 512, 1024, 896, 256, 1024, 640] * 20
         T = list(np.linspace(1.5, 3.5, len(L)))
         rng = np.random.default_rng(3)
         ens = sg.Ensemble(L, T, "ising", 2, seed=3, exchange_every=10)

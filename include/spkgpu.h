@@ -160,7 +160,8 @@ int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_
    update and draws as spkgpu_sweep on an sq/4n lattice without sectors) on a
    lattice the caller keeps in device memory: `spin` holds nx*ny values of
    spin_bytes each (1, 2 or 4; row-major, site index = id-1) and is updated in
-   place; nx and ny must be multiples of 32.  Sweep k uses Philox sweep index
+   place; nx and ny must be multiples of 32 and `spin` 8-byte aligned (as
+   every cudaMalloc pointer is).  Sweep k uses Philox sweep index
    sweep0+k.  The second sweep buffer and the change counter come from one
    static device array of SPKGPU_NOALLOC_MAX_BYTES (+2048) bytes that every
    GPU loading the library holds until exit; larger lattices return

@@ -141,13 +141,14 @@ struct ReplicaCursor {
     j->sweep = sweep;
     j->nspins = a.nspins;
     j->replica = tidx;
-    j->zero_t = 0;
     j->thr = nullptr;
   }
 };
 
+// 16 CTAs of 64 threads per SM (64 registers) for the byte-lane Ising tile;
+// the site-by-site Potts tile keeps more draws live and gets 12 (80)
 template <int APP, typename S>
-__global__ void __launch_bounds__(kTileThreads, 8) ensemble_kernel(EnsArgs a) {
+__global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) ensemble_kernel(EnsArgs a) {
   __shared__ __align__(16) S stage[3][kStageSites];
   __shared__ uint64_t thr[3][5];
   __shared__ unsigned long long red[kTileThreads / 32];

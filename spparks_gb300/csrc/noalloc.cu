@@ -65,6 +65,8 @@ extern "C" int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int3
                                         int32_t nspins, double temperature, uint32_t seed, int64_t sweep0,
                                         int32_t nsweeps, void *stream, int64_t *naccept) {
   if (!spin || nx <= 0 || ny <= 0 || nsweeps < 0 || sweep0 < 0) return SPKGPU_ERR_ARG;
+  // the tile kernel moves site values in 8-byte chunks
+  if ((uintptr_t)spin % 8 != 0) return SPKGPU_ERR_ARG;
   if (app < SPKGPU_ISING || app > SPKGPU_POTTS_NEIGH) return SPKGPU_ERR_ARG;
   if (app == SPKGPU_ISING && nspins != 2) return SPKGPU_ERR_ARG;
   if (nspins < 1 || nspins >= (1 << 21)) return SPKGPU_ERR_ARG;

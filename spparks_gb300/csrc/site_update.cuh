@@ -83,10 +83,13 @@ __device__ __forceinline__ int count_unlike(int v, const int (&nb)[NN]) {
 }
 
 // Philox form: x0 = draw 0 (proposal), x1 = draw 1 (Boltzmann test).
-// thr[dE] in shared or register memory.  Returns the new site value.
+// thr[dE] in shared or register memory.  At zero temperature every thr[dE]
+// is 0, so "x1 < thr" rejects every uphill move, which is the reference's
+// temperature == 0 branch; no separate flag is tested.  Returns the new
+// site value.
 template <int NN, int APP>
 __device__ __forceinline__ int update_philox(int own, const int (&nb)[NN], uint32_t x0, uint32_t x1,
-                                             int nspins, const uint64_t *thr, int zero_t, int *e0_out) {
+                                             int nspins, const uint64_t *thr, int *e0_out) {
   int e0 = count_unlike<NN>(own, nb);
   *e0_out = e0;
   int news;
@@ -115,7 +118,6 @@ __device__ __forceinline__ int update_philox(int own, const int (&nb)[NN], uint3
   // two-state Ising: every neighbour equals either own or news
   int e1 = (APP == SPKGPU_ISING) ? NN - e0 : count_unlike<NN>(news, nb);
   if (e1 <= e0) return news;
-  if (zero_t) return own;
   return ((uint64_t)x1 < thr[e1 - e0]) ? news : own;
 }
 

@@ -29,7 +29,6 @@ __global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
   j.sweep = a.sweep;
   j.nspins = a.nspins;
   j.replica = 0;
-  j.zero_t = a.acc.zero_t;
   j.thr = thr;
   tile_stage_async<S>(j, stage);
   cp_async_commit();

@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(256) phase_kernel(PhaseArgs a) {
       U4 w = sweep_block(a.seed, (uint64_t)i, a.sweep, a.pass);
       uint32_t x0 = (i & 1) ? w.z : w.x;
       uint32_t x1 = (i & 1) ? w.w : w.y;
-      news = update_philox<NN, APP>(own, nb, x0, x1, a.nspins, thr, a.acc.zero_t, &e0);
+      news = update_philox<NN, APP>(own, nb, x0, x1, a.nspins, thr, &e0);
     } else {
       int pm = a.siteseeds[i];
       news = update_strict<NN, APP>(own, nb, pm, a.nspins, pexp, a.acc.zero_t, &e0);

@@ -50,10 +50,10 @@ __device__ __forceinline__ uint32_t first_appearance_small(int own, const int (&
 
 template <int NN, int APP, bool SMALLQ>
 __device__ __forceinline__ int update_rows(int own, const int (&nb)[NN], uint32_t x0, uint32_t x1, int nspins,
-                                           const uint64_t *thr, int zero_t) {
+                                           const uint64_t *thr) {
   if (APP == SPKGPU_ISING || APP == SPKGPU_POTTS) {
     int e0;
-    return update_philox<NN, APP>(own, nb, x0, x1, nspins, thr, zero_t, &e0);
+    return update_philox<NN, APP>(own, nb, x0, x1, nspins, thr, &e0);
   }
   int e0 = count_unlike<NN>(own, nb);
   // no unlike neighbour: no event and no draw (nevent == 0 below)
@@ -72,8 +72,7 @@ __device__ __forceinline__ int update_rows(int own, const int (&nb)[NN], uint32_
   int news = pick_value<NN>(nb, __fns(first, 0, (int)iran + 1));
   int e1 = count_unlike<NN>(news, nb);
   if (e1 <= e0) return news;
-  if (zero_t) return own;
-  return ((uint64_t)x1 < thr[e1 - e0]) ? news : own;
+  return ((uint64_t)x1 < thr[e1 - e0]) ? news : own;  // thr is all 0 at zero temperature
 }
 
 struct RowArgs {
@@ -147,7 +146,7 @@ __global__ void __launch_bounds__(512) row_pair_kernel(RowArgs a) {
         nb[j] = rows[r * nx + xn];
       }
       int own = rows[center * nx + x];
-      int news = update_rows<NN, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr, a.acc.zero_t);
+      int news = update_rows<NN, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr);
       if (news != own) {
         rows[center * nx + x] = (S)news;
         spin[rowbase + x] = (S)news;

@@ -9,9 +9,13 @@
 // its post-phase state.  The tile is read from `src` and written to `dst`
 // (double buffering), so tiles never observe each other's writes.
 //
-// Each thread owns four x-pairs of the tile; the Philox block of a pair is
-// computed once per sweep and serves the colour-1 site of the pair in the
-// first phase and the colour-2 site in the second.
+// The Philox block of an x-pair is computed once per sweep and serves the
+// colour-1 site of the pair in the first phase and the colour-2 site in the
+// second.  A tile has 64 threads and each owns eight x-pairs: for Ising on
+// int8 site values they are two 8-site row segments, updated as eight byte
+// lanes of a 64-bit word (tile_segments_ising8); otherwise eight pairs of
+// one column updated site by site (tile_pairs_sq4).  With 64 threads every
+// thread also updates exactly one ring site, so the first phase is balanced.
 #pragma once
 
 #include <stdint.h>
@@ -23,12 +27,13 @@ namespace spk {
 
 constexpr int kTile = 32;             // tile edge (sites)
 constexpr int kHalo = 2;              // halo rows of one fused sq/4n sweep
-constexpr int kTileThreads = 128;     // threads per tile
-constexpr int kPairsPerThread = kTile * kTile / 2 / kTileThreads;  // 4
-// the stage holds rows y0-2 .. y0+33 and columns x0-4 .. x0+35: four halo
-// columns instead of two so that every staged row is whole 32-bit words
-constexpr int kXOff = 4;
-constexpr int kStageX = kTile + 2 * kXOff;  // 40
+constexpr int kTileThreads = 64;      // threads per tile
+constexpr int kPairsPerThread = kTile * kTile / 2 / kTileThreads;  // 8
+// the stage holds rows y0-2 .. y0+33 and columns x0-8 .. x0+39: eight halo
+// columns instead of two so that staged rows are whole 8-byte chunks and
+// every 8-site row segment of the tile starts on an 8-byte boundary
+constexpr int kXOff = 8;
+constexpr int kStageX = kTile + 2 * kXOff;  // 48
 constexpr int kStageY = kTile + 2 * kHalo;  // 36
 constexpr int kStageSites = kStageX * kStageY;
 // colour-1 sites one step outside the tile that a colour-2 site of the tile
@@ -48,8 +53,7 @@ struct TileJob {
   uint32_t seed, key1, sweep;
   int nspins;
   int replica;        // ensemble: temperature index of the tile's replica
-  int zero_t;
-  const uint64_t *thr;  // thr[dE], dE = 0..4
+  const uint64_t *thr;  // thr[dE], dE = 0..4 (all 0 at zero temperature)
 };
 
 __device__ __forceinline__ int stage_at(int lx, int ly) { return (ly + kHalo) * kStageX + lx + kXOff; }
@@ -57,7 +61,7 @@ __device__ __forceinline__ int stage_at(int lx, int ly) { return (ly + kHalo) * 
 // update one site of the stage in place; returns 1 if its value changed
 template <int APP, typename S>
 __device__ __forceinline__ int site4(S *stage, int lx, int ly, uint32_t x0, uint32_t x1, int nspins,
-                                     const uint64_t *thr, int zero_t) {
+                                     const uint64_t *thr) {
   // neighbour order of sq/4n: x-1, y-1, y+1, x+1 (src/create_sites.cpp:1313-1330)
   const int c = stage_at(lx, ly);
   int own = stage[c];
@@ -67,7 +71,7 @@ __device__ __forceinline__ int site4(S *stage, int lx, int ly, uint32_t x0, uint
   nb[2] = stage[c + kStageX];
   nb[3] = stage[c + 1];
   int e0;
-  int news = update_philox<4, APP>(own, nb, x0, x1, nspins, thr, zero_t, &e0);
+  int news = update_philox<4, APP>(own, nb, x0, x1, nspins, thr, &e0);
   if (news != own) {
     stage[c] = (S)news;
     return 1;
@@ -75,23 +79,24 @@ __device__ __forceinline__ int site4(S *stage, int lx, int ly, uint32_t x0, uint
   return 0;
 }
 
-// Issue the staging of a tile (tile + halo, periodic wrap) as 4-byte
+// Issue the staging of a tile (tile + halo, periodic wrap) as 8-byte
 // cp.async copies into `stage`; the caller commits, waits and synchronises
-// before tile_sweep_sq4 reads it.  Word columns never straddle the wrap: x0
-// and L are multiples of 32.
+// before tile_sweep_sq4 reads it.  Chunks never straddle the wrap: x0 and L
+// are multiples of 32 and a chunk holds at most 8 sites.
 template <typename S>
 __device__ __forceinline__ void tile_stage_async(const TileJob &j, S *stage) {
-  constexpr int VEC = 4 / (int)sizeof(S);  // sites per 32-bit word
-  constexpr int WPR = kStageX / VEC;       // words per staged row
+  constexpr int VEC = 8 / (int)sizeof(S);  // sites per 8-byte chunk
+  constexpr int CPR = kStageX / VEC;       // chunks per staged row
+  static_assert(kXOff % VEC == 0 && kStageX % VEC == 0, "staged rows are whole chunks");
   const S *src = (const S *)j.src;
-  for (int k = threadIdx.x; k < kStageY * WPR; k += kTileThreads) {
-    int ly = k / WPR, wc = k - ly * WPR;
+  for (int k = threadIdx.x; k < kStageY * CPR; k += kTileThreads) {
+    int ly = k / CPR, wc = k - ly * CPR;
     int gy = j.y0 + ly - kHalo, gx = j.x0 - kXOff + wc * VEC;
     gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
     gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
     const void *g = src + (int64_t)gy * j.L + gx;
     unsigned sa = (unsigned)__cvta_generic_to_shared(stage + ly * kStageX + wc * VEC);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(g) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(g) : "memory");
   }
 }
 
@@ -99,13 +104,39 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// One fused sweep of a staged tile (tile_stage_async, committed, waited for
-// and followed by __syncthreads).  The stage buffer of this tile must not be
-// the one the next tile is being staged into.  Returns the number of site
-// values changed inside the tile.
+// ring: colour-1 sites one step outside the tile that a colour-2 site of the
+// tile neighbours, one per thread tid < kRing (their owners compute the same
+// values from the same draws)
 template <int APP, typename S>
-__device__ __forceinline__ int tile_sweep_sq4(const TileJob &j, S *stage) {
-  constexpr int VEC = 4 / (int)sizeof(S);  // sites per 32-bit word
+__device__ __forceinline__ void ring_site(const TileJob &j, S *stage, const RoundKeys &rk, int tid) {
+  int q = tid & (kTile / 2 - 1);
+  int rlx, rly;
+  if (tid < kTile / 2) {               // row -1: lx odd in [1, 31]
+    rly = -1;
+    rlx = 2 * q + 1;
+  } else if (tid < kTile) {            // row 32: lx even in [0, 30]
+    rly = kTile;
+    rlx = 2 * q;
+  } else if (tid < 3 * kTile / 2) {    // column -1: ly odd
+    rlx = -1;
+    rly = 2 * q + 1;
+  } else {                             // column 32: ly even
+    rlx = kTile;
+    rly = 2 * q;
+  }
+  int gy = j.y0 + rly, gx = j.x0 + rlx;
+  gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
+  gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
+  int64_t s = j.base + (int64_t)gy * j.L + gx;
+  U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), j.sweep, 0u}, rk);
+  uint32_t a0 = (s & 1) ? w.z : w.x, a1 = (s & 1) ? w.w : w.y;
+  site4<APP, S>(stage, rlx, rly, a0, a1, j.nspins, j.thr);
+}
+
+// Site-by-site form: thread tid owns the x-pairs p = tid + k*kTileThreads,
+// row p/16, sites 2(p%16) and 2(p%16)+1.
+template <int APP, typename S>
+__device__ __forceinline__ int tile_pairs_sq4(const TileJob &j, S *stage) {
   S *dst = (S *)j.dst;
   const int tid = threadIdx.x;
   const RoundKeys rk = round_keys(j.seed, j.key1);
@@ -123,51 +154,148 @@ __device__ __forceinline__ int tile_sweep_sq4(const TileJob &j, S *stage) {
     uint32_t a0 = h ? w.z : w.x, a1 = h ? w.w : w.y;
     keep0[k] = h ? w.x : w.z;
     keep1[k] = h ? w.y : w.w;
-    changed += site4<APP, S>(stage, 2 * m + h, ly, a0, a1, j.nspins, j.thr, j.zero_t);
+    changed += site4<APP, S>(stage, 2 * m + h, ly, a0, a1, j.nspins, j.thr);
   }
-  // ring: colour-1 sites one step outside the tile (their owners compute the
-  // same values from the same draws)
-  if (tid < kRing) {
-    int q = tid & (kTile / 2 - 1);
-    int rlx, rly;
-    if (tid < kTile / 2) {               // row -1: lx odd in [1, 31]
-      rly = -1;
-      rlx = 2 * q + 1;
-    } else if (tid < kTile) {            // row 32: lx even in [0, 30]
-      rly = kTile;
-      rlx = 2 * q;
-    } else if (tid < 3 * kTile / 2) {    // column -1: ly odd
-      rlx = -1;
-      rly = 2 * q + 1;
-    } else {                             // column 32: ly even
-      rlx = kTile;
-      rly = 2 * q;
-    }
-    int gy = j.y0 + rly, gx = j.x0 + rlx;
-    gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
-    gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
-    int64_t s = j.base + (int64_t)gy * j.L + gx;
-    U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), j.sweep, 0u}, rk);
-    uint32_t a0 = (s & 1) ? w.z : w.x, a1 = (s & 1) ? w.w : w.y;
-    site4<APP, S>(stage, rlx, rly, a0, a1, j.nspins, j.thr, j.zero_t);
-  }
+  if (tid < kRing) ring_site<APP, S>(j, stage, rk, tid);
   __syncthreads();
-  // phase 2: colour-2 sites, in place, seeing every colour-1 neighbour updated
+  // phase 2: colour-2 sites, seeing every colour-1 neighbour updated; each
+  // thread then writes its own x-pairs (both values are final) to dst, so no
+  // barrier is needed before the next tile (it stages into another buffer)
 #pragma unroll
   for (int k = 0; k < kPairsPerThread; k++) {
     int p = tid + k * kTileThreads;
     int ly = p >> 4, m = p & 15;
-    changed += site4<APP, S>(stage, 2 * m + 1 - (ly & 1), ly, keep0[k], keep1[k], j.nspins, j.thr, j.zero_t);
-  }
-  __syncthreads();
-  // write the tile interior as 32-bit words
-  constexpr int WROW = kTile / VEC;
-  for (int k = tid; k < kTile * WROW; k += kTileThreads) {
-    int ly = k / WROW, wc = k - ly * WROW;
-    uint32_t v = *(const uint32_t *)(stage + stage_at(wc * VEC, ly));
-    *(uint32_t *)(dst + (int64_t)(j.y0 + ly) * j.L + j.x0 + wc * VEC) = v;
+    int h = ly & 1;  // the pair's colour-1 site
+    changed += site4<APP, S>(stage, 2 * m + 1 - h, ly, keep0[k], keep1[k], j.nspins, j.thr);
+    S v0 = stage[stage_at(2 * m, ly)], v1 = stage[stage_at(2 * m + 1, ly)];
+    S *out = dst + (int64_t)(j.y0 + ly) * j.L + j.x0 + 2 * m;
+    if (sizeof(S) == 1) {
+      *(uint16_t *)out = (uint16_t)((uint8_t)v0 | ((uint16_t)(uint8_t)v1 << 8));
+    } else if (sizeof(S) == 2) {
+      *(uint32_t *)out = (uint32_t)(uint16_t)v0 | ((uint32_t)(uint16_t)v1 << 16);
+    } else {
+      *(uint64_t *)out = (uint64_t)(uint32_t)v0 | ((uint64_t)(uint32_t)v1 << 32);
+    }
   }
   return changed;
+}
+
+// ---- Ising on int8 site values, eight byte lanes per 64-bit word ----------
+//
+// A lane holds a site value, 1 or 2; its bit 0 (1 for value 1, 0 for value
+// 2) tells the two states apart, so the number of unlike neighbours e0 is the
+// sum of four XORs of bit 0, at most 4 per lane (no carry between lanes).
+// AppIsing::site_event_rejection (src/app_ising.cpp:104-136) then reads:
+// draw 0 proposes value 1 iff x0 < 2^31-1; a proposal equal to the current
+// value changes nothing; otherwise e1 = 4 - e0, the flip is taken iff
+// e1 <= e0 (e0 >= 2) or x1 < thr[e1-e0] with e1-e0 = 2 (e0 = 1) or 4
+// (e0 = 0).  Each site's draws are folded into a lane code
+//   lvl + 4*p,  lvl = [x1 < thr[4]] + [x1 < thr[2]],  p = [x0 < 2^31-1]
+// (thr[4] <= thr[2], so lvl >= 2 - e0 <=> the Boltzmann test passes for that
+// e0), and the flip condition becomes e0 + lvl >= 2 and p != bit 0, both
+// evaluated for all lanes at once.  At zero temperature thr[] is all zero,
+// so lvl = 0 and only e0 >= 2 flips.
+constexpr uint64_t kLaneBit = 0x0101010101010101ull;
+constexpr uint64_t kEvenLanes = 0x0001000100010001ull;  // bit 0 of lanes 0, 2, 4, 6
+constexpr uint64_t kOddLanes = 0x0100010001000100ull;   // bit 0 of lanes 1, 3, 5, 7
+constexpr int kSegPerThread = kTile * kTile / 8 / kTileThreads;  // 8-site segments
+static_assert(kSegPerThread * 4 == kPairsPerThread, "a segment holds four x-pairs");
+static_assert(kSegPerThread * 8 * kTileThreads == kTile * kTile, "segments must cover the tile");
+
+// lane code of one site from its two draws
+__device__ __forceinline__ uint32_t ising_lane_code(uint32_t x0, uint32_t x1, uint64_t t2, uint64_t t4) {
+  return (uint32_t)((uint64_t)x1 < t4) + (uint32_t)((uint64_t)x1 < t2) + (x0 < 0x7FFFFFFFu ? 4u : 0u);
+}
+
+// unlike-neighbour counts of the eight lanes of the segment at stage index c
+// (8-byte aligned); v receives the segment itself
+__device__ __forceinline__ uint64_t seg_unlike(const int8_t *stage, int c, uint64_t &v) {
+  v = *(const uint64_t *)(stage + c);
+  const uint64_t up = *(const uint64_t *)(stage + c - kStageX);
+  const uint64_t dn = *(const uint64_t *)(stage + c + kStageX);
+  const uint64_t lb = (uint8_t)stage[c - 1], rb = (uint8_t)stage[c + 8];
+  const uint64_t b = v & kLaneBit;
+  const uint64_t l = ((v << 8) | lb) & kLaneBit;          // lane i: site x-1
+  const uint64_t r = ((v >> 8) | (rb << 56)) & kLaneBit;  // lane i: site x+1
+  return (b ^ l) + (b ^ (up & kLaneBit)) + (b ^ (dn & kLaneBit)) + (b ^ r);
+}
+
+// lanes (bit 0) of `cmask` that flip, given unlike counts e, segment v, codes lv
+__device__ __forceinline__ uint64_t seg_flips(uint64_t e, uint64_t v, uint64_t lv, uint64_t cmask) {
+  const uint64_t acc = (((e + (lv & 0x0303030303030303ull)) + 0x7E7E7E7E7E7E7E7Eull) >> 7) & kLaneBit;
+  const uint64_t p = (lv >> 2) & kLaneBit;
+  return (p ^ v) & acc & cmask;
+}
+
+template <typename S>
+__device__ __forceinline__ int tile_segments_ising8(const TileJob &j, S *stage_s) {
+  static_assert(sizeof(S) == 1, "byte lanes");
+  int8_t *stage = (int8_t *)stage_s;
+  int8_t *dst = (int8_t *)j.dst;
+  const int tid = threadIdx.x;
+  const RoundKeys rk = round_keys(j.seed, j.key1);
+  const uint64_t t2 = j.thr[2], t4 = j.thr[4];
+  int changed = 0;
+  uint64_t lv[kSegPerThread];
+  // draws: the four x-pairs of each segment
+#pragma unroll
+  for (int k = 0; k < kSegPerThread; k++) {
+    const int g = tid + k * kTileThreads;
+    const int ly = g >> 2, x0 = (g & 3) * 8;
+    const int64_t s = j.base + (int64_t)(j.y0 + ly) * j.L + j.x0 + x0;  // even
+    uint64_t code = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int64_t pr = (s >> 1) + i;
+      U4 w = philox4x32_10_rk(U4{(uint32_t)pr, (uint32_t)(pr >> 32), j.sweep, 0u}, rk);
+      uint32_t c2 = ising_lane_code(w.x, w.y, t2, t4) | (ising_lane_code(w.z, w.w, t2, t4) << 8);
+      code |= (uint64_t)c2 << (16 * i);
+    }
+    lv[k] = code;
+  }
+  // phase 1: colour-1 lanes (lane parity == row parity), in place
+#pragma unroll
+  for (int k = 0; k < kSegPerThread; k++) {
+    const int g = tid + k * kTileThreads;
+    const int ly = g >> 2, x0 = (g & 3) * 8;
+    const int c = stage_at(x0, ly);
+    uint64_t v;
+    const uint64_t e = seg_unlike(stage, c, v);
+    const uint64_t f = seg_flips(e, v, lv[k], (ly & 1) ? kOddLanes : kEvenLanes);
+    if (f) {
+      *(uint64_t *)(stage + c) = v ^ (f | (f << 1));  // 1 <-> 2
+      changed += __popcll(f);
+    }
+  }
+  if (tid < kRing) ring_site<SPKGPU_ISING, S>(j, stage_s, rk, tid);
+  __syncthreads();
+  // phase 2: colour-2 lanes, seeing every colour-1 neighbour updated; the
+  // segment is then final and goes straight to dst
+#pragma unroll
+  for (int k = 0; k < kSegPerThread; k++) {
+    const int g = tid + k * kTileThreads;
+    const int ly = g >> 2, x0 = (g & 3) * 8;
+    const int c = stage_at(x0, ly);
+    uint64_t v;
+    const uint64_t e = seg_unlike(stage, c, v);
+    const uint64_t f = seg_flips(e, v, lv[k], (ly & 1) ? kEvenLanes : kOddLanes);
+    changed += __popcll(f);
+    *(uint64_t *)(dst + (int64_t)(j.y0 + ly) * j.L + j.x0 + x0) = v ^ (f | (f << 1));
+  }
+  return changed;
+}
+
+// One fused sweep of a staged tile (tile_stage_async, committed, waited for
+// and followed by __syncthreads).  The stage buffer of this tile must not be
+// the one the next tile is being staged into, and a thread may return while
+// others still read this tile's stage: callers synchronise before reusing it.
+// Returns the number of site values changed inside the tile.
+template <int APP, typename S>
+__device__ __forceinline__ int tile_sweep_sq4(const TileJob &j, S *stage) {
+  if constexpr (APP == SPKGPU_ISING && sizeof(S) == 1)
+    return tile_segments_ising8<S>(j, stage);
+  else
+    return tile_pairs_sq4<APP, S>(j, stage);
 }
 
 }  // namespace spk

@@ -70,3 +70,22 @@ def test_null_handle_calls_fail_cleanly(lib):
     assert lib.spkgpu_sweep(None, 1) == -1
     assert lib.spkgpu_destroy(None) == -1
     assert lib.spkgpu_last_error(None) == b"null handle"
+
+
+def test_noalloc_rejects_bad_arguments_before_any_device_call(lib):
+    f = lib.spkgpu_sweep_sq4_noalloc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                  ctypes.c_int32, ctypes.c_double, ctypes.c_uint32, ctypes.c_int64, ctypes.c_int32,
+                  ctypes.c_void_p, ctypes.c_void_p]
+    # (pointer, nx, ny, spin_bytes, app, nspins, T): never dereferenced on these paths
+    bad = [
+        (0x10000, 64, 64, 1, sg.ISING, 2, -1.0),     # negative temperature
+        (0x10004, 64, 64, 1, sg.ISING, 2, 2.0),      # not 8-byte aligned
+        (0x10000, 48, 64, 1, sg.ISING, 2, 2.0),      # extent not a multiple of 32
+        (0x10000, 64, 64, 1, sg.ISING, 3, 2.0),      # Ising is two-state
+        (0x10000, 64, 64, 3, sg.POTTS, 5, 2.0),      # no 3-byte site values
+        (None, 64, 64, 1, sg.ISING, 2, 2.0),
+    ]
+    for p, nx, ny, sb, app, q, T in bad:
+        assert f(p, nx, ny, sb, app, q, T, 1, 0, 1, None, None) == -1, (p, nx, ny, sb, app, q, T)

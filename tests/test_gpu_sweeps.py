@@ -79,11 +79,16 @@ RANDOM_CASES = [
     dict(lattice="sc/26n", nx=10, ny=8, nz=6, app="potts/neigh", nspins=7, temperature=1.3),
     dict(lattice="sq/4n", nx=32, ny=32, nz=1, app="ising", nspins=2, temperature=1.1345, nsector=4),
     dict(lattice="sc/6n", nx=12, ny=12, nz=12, app="potts", nspins=5, temperature=0.7, nsector=8),
+    # zero temperature: every uphill move rejected (src/app_potts.cpp:128)
+    dict(lattice="sq/8n", nx=40, ny=24, nz=1, app="potts", nspins=12, temperature=0.0),
+    dict(lattice="sc/26n", nx=12, ny=10, nz=8, app="potts/neighonly", nspins=40, temperature=0.0),
+    dict(lattice="sq/4n", nx=64, ny=32, nz=1, app="potts/neigh", nspins=6, temperature=0.0),
 ]
 
 
 @pytest.mark.parametrize("variant", [0, 1])
-@pytest.mark.parametrize("case", RANDOM_CASES, ids=lambda c: f"{c['app']}-{c['lattice']}-{c.get('nsector', 1)}")
+@pytest.mark.parametrize("case", RANDOM_CASES,
+                         ids=lambda c: f"{c['app']}-{c['lattice']}-{c.get('nsector', 1)}-T{c['temperature']}")
 def test_random_cases_match_oracle(sg, case, variant):
     """variant 0 takes the fastest kernel (fused tile, row-pair or packed),
     variant 1 always the per-colour phase kernel."""
