@@ -179,9 +179,14 @@ int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int32_t spin_by
 
 /* batched ensemble of independent sq/4n lattices ---------------------------
    Many replicas of uneven size L x L (L a multiple of 32) and their own
-   temperatures swept together by one persistent cooperative kernel, with
-   parallel-tempering replica exchange between neighbouring temperatures of
-   equal-L replicas every exchange_every sweeps, on the device.  Each replica
+   temperatures swept together, with parallel-tempering replica exchange
+   between neighbouring temperatures of equal-L replicas every exchange_every
+   sweeps, on the device.  Two execution forms give identical results: one
+   persistent cooperative kernel per step (sweeps separated by a bounded grid
+   barrier), or one launch per sweep over every tile of every replica with
+   the exchange as separate launches; create times one captured step of each
+   on the replica set and keeps the faster (SPKGPU_ENSEMBLE_MODE=persistent or
+   =launches in the environment forces one).  Each replica
    follows the same per-site rule as a single `sweep color` lattice (same as
    spkgpu_sweep with sq/4n); replica r draws from Philox stream (r+1) << 8.
    The reference has no ensemble; it corresponds to running one reference
@@ -210,8 +215,8 @@ int spkgpu_ensemble_destroy(spkgpu_ensemble *e);
 const char *spkgpu_ensemble_last_error(const spkgpu_ensemble *e);
 int spkgpu_ensemble_upload(spkgpu_ensemble *e, const int32_t *spin, int64_t n);
 int spkgpu_ensemble_download(spkgpu_ensemble *e, int32_t *spin, int64_t n);
-/* enqueue nsweeps sweeps (a multiple of exchange_every when exchanging);
-   runs as replays of a captured CUDA graph of one persistent launch */
+/* enqueue nsweeps sweeps; whole exchange periods run as replays of a
+   captured CUDA graph of one step */
 int spkgpu_ensemble_run(spkgpu_ensemble *e, int32_t nsweeps);
 int spkgpu_ensemble_timed_run(spkgpu_ensemble *e, int32_t nsweeps, float *ms);
 int spkgpu_ensemble_synchronize(spkgpu_ensemble *e);
@@ -221,6 +226,15 @@ int spkgpu_ensemble_get_stats(spkgpu_ensemble *e, spkgpu_ensemble_stats *out);
 int spkgpu_ensemble_temperatures(spkgpu_ensemble *e, double *temperature);
 int spkgpu_ensemble_energies(spkgpu_ensemble *e, int64_t *bonds);
 int spkgpu_ensemble_launch_count(const spkgpu_ensemble *e, int64_t *count);
+/* execution form in use and the autotuner's time of one step in each form
+   (tune_ms[2], ms; -1 where not timed); tune_ms may be NULL */
+#define SPKGPU_ENSEMBLE_PERSISTENT 0
+#define SPKGPU_ENSEMBLE_LAUNCHES 1
+int spkgpu_ensemble_mode(const spkgpu_ensemble *e, int32_t *mode, float *tune_ms);
+/* device time (ms) of the sweep kernels in the most recent replay of the
+   captured step and how many launches that covers (1 persistent kernel, or
+   one launch per sweep); waits for that replay */
+int spkgpu_ensemble_sweep_kernel_ms(spkgpu_ensemble *e, float *ms, int32_t *nlaunch);
 
 #ifdef __cplusplus
 }

@@ -99,7 +99,8 @@ EXPORTS = [
     "spkgpu_ensemble_create", "spkgpu_ensemble_destroy", "spkgpu_ensemble_last_error", "spkgpu_ensemble_upload",
     "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
     "spkgpu_ensemble_get_stats", "spkgpu_ensemble_temperatures", "spkgpu_ensemble_energies",
-    "spkgpu_ensemble_launch_count", "spkgpu_sweep_sq4_noalloc",
+    "spkgpu_ensemble_launch_count", "spkgpu_ensemble_mode", "spkgpu_ensemble_sweep_kernel_ms",
+    "spkgpu_sweep_sq4_noalloc",
     "spparks_open_no_mpi", "spparks_close", "spparks_file", "spparks_command", "spparks_extract", "spparks_energy",
     "spkgpu_driver_error", "spkgpu_driver_time",
 ]
@@ -153,6 +154,8 @@ def load_library(path: Path | None = None):
     L.spkgpu_ensemble_temperatures.argtypes = [vp, P(ctypes.c_double)]
     L.spkgpu_ensemble_energies.argtypes = [vp, P(ctypes.c_int64)]
     L.spkgpu_ensemble_launch_count.argtypes = [vp, P(ctypes.c_int64)]
+    L.spkgpu_ensemble_mode.argtypes = [vp, P(ctypes.c_int32), P(ctypes.c_float)]
+    L.spkgpu_ensemble_sweep_kernel_ms.argtypes = [vp, P(ctypes.c_float), P(ctypes.c_int32)]
     L.spkgpu_sweep_sq4_noalloc.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_int32, ctypes.c_double, ctypes.c_uint32, ctypes.c_int64,
                                            ctypes.c_int32, vp, P(ctypes.c_int64)]
@@ -352,6 +355,23 @@ class Ensemble:
         self._check(self.lib.spkgpu_ensemble_get_stats(self.h, ctypes.byref(s)))
         return {"naccept": s.naccept, "nattempt": s.nattempt, "nsweeps": s.nsweeps,
                 "exchange_tries": s.exchange_tries, "exchange_accepts": s.exchange_accepts}
+
+    def mode(self) -> dict:
+        """Execution form the autotuner kept ("persistent" or "launches") and
+        its time of one step in each form (ms, None where not timed)."""
+        m = ctypes.c_int32()
+        ms = (ctypes.c_float * 2)()
+        self._check(self.lib.spkgpu_ensemble_mode(self.h, ctypes.byref(m), ms))
+        names = ("persistent", "launches")
+        return {"mode": names[m.value],
+                "tune_ms": {names[k]: (float(ms[k]) if ms[k] >= 0 else None) for k in range(2)}}
+
+    def sweep_kernel_ms(self):
+        """(ms, launches): device time of the sweep kernels in the last replay
+        of the captured step, and how many launches that time covers."""
+        ms, n = ctypes.c_float(), ctypes.c_int32()
+        self._check(self.lib.spkgpu_ensemble_sweep_kernel_ms(self.h, ctypes.byref(ms), ctypes.byref(n)))
+        return float(ms.value), int(n.value)
 
     def temperatures(self) -> np.ndarray:
         out = np.empty(len(self.L), dtype=np.float64)

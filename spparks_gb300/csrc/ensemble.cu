@@ -18,14 +18,18 @@
 #include <cuda/atomic>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <string>
 #include <vector>
 
+#include "counters.cuh"
 #include "spk_internal.h"
 #include "tile_sweep.cuh"
 
@@ -49,12 +53,15 @@ struct EnsArgs {
   const int32_t *L;
   const int64_t *base;
   const int32_t *tile_start;    // nrep+1 prefix of tiles per replica
+  const int32_t *tile_rep;      // replica of each tile (launch-per-sweep mode)
+  const int2 *tile_pos;         // {replica, (y0/32) << 16 | x0/32} of each tile
   int nrep, ntiles;
   int32_t *tidx;                // replica -> temperature index
   const uint64_t *thr;          // [ntemp][5]
   const double *beta;           // [ntemp]
   const int32_t *group_start;   // ngroups+1 prefix of slots
   const int32_t *slot_t;        // temperature index of each slot (ascending T)
+  const int32_t *slot_group;    // group of each slot
   int32_t *who;                 // replica in each slot
   unsigned long long *bonds;    // per replica, accumulated at an exchange
   long long *last_bonds;        // per replica, copy at the last exchange
@@ -64,6 +71,7 @@ struct EnsArgs {
   int nspins;
   uint32_t seed;
   EnsCtl *ctl;
+  unsigned long long *nacc_slots;  // kCounterSlots change counters (launch-per-sweep mode)
 };
 
 constexpr long long kBarrierSpinLimit = 1LL << 25;  // ~seconds with nanosleep: then give up
@@ -107,6 +115,86 @@ __device__ __forceinline__ int replica_of_tile(const int32_t *tile_start, int nr
     else hi = mid;
   }
   return lo;
+}
+
+// adds the unlike bonds (right and down neighbour of each site) of tile t of
+// replica r in `curbuf` to a.bonds[r]; every thread of the block calls it.
+// int8 sites, eight per 64-bit word: a byte lane is "unlike" where the XOR
+// with the neighbour word is non-zero.
+__device__ __forceinline__ uint64_t lanes_nonzero(uint64_t d) {
+  return ((d & 0x7F7F7F7F7F7F7F7Full) + 0x7F7F7F7F7F7F7F7Full | d) & 0x8080808080808080ull;
+}
+
+template <typename S>
+__device__ void tile_bonds(const EnsArgs &a, int t, int r, const S *curbuf) {
+  static_assert(sizeof(S) == 1, "ensemble sites are int8");
+  const int L = a.L[r];
+  const int tpr = L / kTile;
+  const int lt = t - a.tile_start[r];
+  const int x0 = (lt % tpr) * kTile, y0 = (lt / tpr) * kTile;
+  const uint8_t *rep = (const uint8_t *)curbuf + a.base[r];
+  unsigned int b = 0;
+  // 128 segments of 8 sites per tile
+  for (int g = threadIdx.x; g < kTile * kTile / 8; g += kTileThreads) {
+    const int y = y0 + (g >> 2), x = x0 + (g & 3) * 8;
+    const int xr = x + 8 == L ? 0 : x + 8;
+    const int yd = y + 1 == L ? 0 : y + 1;
+    const uint64_t v = *(const uint64_t *)(rep + (int64_t)y * L + x);
+    const uint64_t dn = *(const uint64_t *)(rep + (int64_t)yd * L + x);
+    const uint64_t rb = rep[(int64_t)y * L + xr];
+    const uint64_t right = (v >> 8) | (rb << 56);
+    b += __popcll(lanes_nonzero(v ^ right)) + __popcll(lanes_nonzero(v ^ dn));
+  }
+  unsigned int w = __reduce_add_sync(0xFFFFFFFFu, b);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(&a.bonds[r], (unsigned long long)w);
+}
+
+// exchange round `xround` over all groups, by every thread of one block,
+// once the bonds of every replica are complete: in a round the slot pairs
+// (j, j+1), j - group start = xround mod 2, are disjoint, so each thread
+// takes pairs on its own.  Swaps the temperatures of accepted pairs, keeps
+// the bonds as last_bonds and clears them.
+__device__ void exchange_round(const EnsArgs &a, uint32_t xround) {
+  __shared__ unsigned int cnt[2];
+  if (threadIdx.x == 0) cnt[0] = cnt[1] = 0;
+  __syncthreads();
+  unsigned int tries = 0, acc = 0;
+  const int n = a.nrep;
+  for (int jj = threadIdx.x; jj < n; jj += blockDim.x) {
+    const int g = a.slot_group[jj];
+    const int lo = a.group_start[g], hi = a.group_start[g + 1];
+    if (((jj - lo) & 1) != (int)(xround & 1u) || jj + 1 >= hi) continue;
+    int ra = a.who[jj], rb = a.who[jj + 1];
+    int ta = a.slot_t[jj], tb = a.slot_t[jj + 1];
+    double delta = (a.beta[ta] - a.beta[tb]) * ((double)a.bonds[ra] - (double)a.bonds[rb]);
+    U4 w = philox4x32_10(U4{xround, (uint32_t)g, (uint32_t)(jj - lo), 0u}, a.seed, kStreamExchange);
+    bool accept = delta >= 0.0;
+    if (!accept) {
+      double p = exp(delta) * 4294967296.0;
+      accept = (double)w.x < floor(p);
+    }
+    tries++;
+    if (accept) {
+      a.who[jj] = rb;
+      a.who[jj + 1] = ra;
+      a.tidx[ra] = tb;
+      a.tidx[rb] = ta;
+      acc++;
+    }
+  }
+  if (tries) atomicAdd(&cnt[0], tries);
+  if (acc) atomicAdd(&cnt[1], acc);
+  __syncthreads();  // every pair read its bonds before they are cleared
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    a.last_bonds[r] = (long long)a.bonds[r];
+    a.bonds[r] = 0;
+  }
+  if (threadIdx.x == 0) {
+    a.ctl->xtries += cnt[0];
+    a.ctl->xaccepts += cnt[1];
+  }
+  __threadfence();
+  __syncthreads();
 }
 
 // walks the tiles of a contiguous range, keeping the current replica's
@@ -171,18 +259,24 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
     const int t1 = (int)(((int64_t)a.ntiles * (blockIdx.x + 1)) / gridDim.x);
     const uint32_t sweep = sweep0 + (uint32_t)s;
     ReplicaCursor rc;
-    if (t0 < t1) rc.seek(a, t0);
-    TileJob cur, nxt;
-    int sb = 0;
     if (t0 < t1) {
-      rc.job<S>(a, t0, src, dst, sweep, &cur);
-      tile_stage_async<S>(cur, stage[sb]);
+      rc.seek(a, t0);
+      TileJob first;
+      rc.job<S>(a, t0, src, dst, sweep, &first);
+      tile_stage_async<S>(first, stage[0]);
     }
     cp_async_commit();
+    int sb = 0;
     for (int t = t0; t < t1; t++) {
-      int sn = sb == 2 ? 0 : sb + 1;
+      const int sn = sb == 2 ? 0 : sb + 1;
+      // the job of tile t is rebuilt from the cursor (which the staging of t
+      // left at t's replica) rather than carried over, so only one job is
+      // live while the tile is swept
+      TileJob cur;
+      rc.job<S>(a, t, src, dst, sweep, &cur);
       if (threadIdx.x < 5) thr[sb][threadIdx.x] = a.thr[(int64_t)cur.replica * 5 + threadIdx.x];
       if (t + 1 < t1) {
+        TileJob nxt;
         rc.job<S>(a, t + 1, src, dst, sweep, &nxt);
         tile_stage_async<S>(nxt, stage[sn]);
       }
@@ -191,7 +285,6 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
       __syncthreads();
       cur.thr = thr[sb];
       my_changed += (unsigned long long)tile_sweep_sq4<APP, S>(cur, stage[sb]);
-      cur = nxt;
       sb = sn;
     }
     cp_async_wait<0>();
@@ -202,58 +295,11 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
     if (a.exchange_every > 0 && done % (uint32_t)a.exchange_every == 0) {
       // unlike bonds of each replica (right and down neighbour of each site)
       const S *curbuf = (const S *)(parity ? a.buf1 : a.buf0);
-      for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        int r = replica_of_tile(a.tile_start, a.nrep, t);
-        int L = a.L[r];
-        int tpr = L / kTile;
-        int lt = t - a.tile_start[r];
-        int x0 = (lt % tpr) * kTile, y0 = (lt / tpr) * kTile;
-        const S *rep = curbuf + a.base[r];
-        unsigned int b = 0;
-        for (int k = threadIdx.x; k < kTile * kTile; k += kTileThreads) {
-          int y = y0 + (k >> 5), x = x0 + (k & 31);
-          S v = rep[(int64_t)y * L + x];
-          int xr = x + 1 == L ? 0 : x + 1;
-          int yd = y + 1 == L ? 0 : y + 1;
-          b += (rep[(int64_t)y * L + xr] != v) + (rep[(int64_t)yd * L + x] != v);
-        }
-        unsigned int w = __reduce_add_sync(0xFFFFFFFFu, b);
-        if ((threadIdx.x & 31) == 0 && w) atomicAdd(&a.bonds[r], (unsigned long long)w);
-      }
+      for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x)
+        tile_bonds<S>(a, t, replica_of_tile(a.tile_start, a.nrep, t), curbuf);
       ok = grid_barrier(ctl);
       if (!ok) break;
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
-        unsigned long long tries = 0, acc = 0;
-        for (int g = 0; g < a.ngroups; g++) {
-          int lo = a.group_start[g], hi = a.group_start[g + 1];
-          for (int jj = lo + (int)(xround & 1u); jj + 1 < hi; jj += 2) {
-            int ra = a.who[jj], rb = a.who[jj + 1];
-            int ta = a.slot_t[jj], tb = a.slot_t[jj + 1];
-            double delta = (a.beta[ta] - a.beta[tb]) * ((double)a.bonds[ra] - (double)a.bonds[rb]);
-            U4 w = philox4x32_10(U4{xround, (uint32_t)g, (uint32_t)(jj - lo), 0u}, a.seed, kStreamExchange);
-            bool accept = delta >= 0.0;
-            if (!accept) {
-              double p = exp(delta) * 4294967296.0;
-              accept = (double)w.x < floor(p);
-            }
-            tries++;
-            if (accept) {
-              a.who[jj] = rb;
-              a.who[jj + 1] = ra;
-              a.tidx[ra] = tb;
-              a.tidx[rb] = ta;
-              acc++;
-            }
-          }
-        }
-        for (int r = 0; r < a.nrep; r++) {
-          a.last_bonds[r] = (long long)a.bonds[r];
-          a.bonds[r] = 0;
-        }
-        ctl->xtries += tries;
-        ctl->xaccepts += acc;
-        __threadfence();
-      }
+      if (blockIdx.x == 0) exchange_round(a, xround);
       xround++;
       ok = grid_barrier(ctl);
     }
@@ -272,6 +318,69 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
     ctl->parity = parity;
     ctl->sweep = sweep0 + (uint32_t)a.nsweeps;
     ctl->xround = xround;
+  }
+}
+
+// ---- launch-per-sweep mode ------------------------------------------------
+// (the byte-lane Ising tile fits 32 registers: 32 CTAs of 64 threads per SM;
+// the site-by-site Potts tile gets 80)
+// The same sweep as one launch per sweep: one CTA per tile of every replica
+// (tile -> replica from a table), sweep index ctl->sweep + k and source
+// buffer ctl->parity ^ (k & 1), so that a captured graph of k = 0..m-1 can be
+// replayed; ensemble_advance_kernel then moves ctl on by m sweeps.  Bonds and
+// the exchange round run as their own launches between the last sweep of a
+// period and the advance.
+template <int APP, typename S>
+__global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) ensemble_sweep_kernel(EnsArgs a,
+                                                                                                     int k) {
+  __shared__ __align__(16) S stage[kStageSites];
+  __shared__ uint64_t thr[5];
+  const int2 tp = a.tile_pos[blockIdx.x];
+  const int r = tp.x;
+  const int L = a.L[r];
+  const int parity = *(volatile int *)&a.ctl->parity ^ (k & 1);
+  const int64_t base = a.base[r];
+  const int tix = a.tidx[r];
+  TileJob j;
+  j.src = (const S *)(parity ? a.buf1 : a.buf0) + base;
+  j.dst = (S *)(parity ? a.buf0 : a.buf1) + base;
+  j.L = L;
+  j.Ly = L;
+  j.x0 = (tp.y & 0xFFFF) * kTile;
+  j.y0 = (tp.y >> 16) * kTile;
+  j.base = 0;  // replicas differ by Philox stream word; site counter is local
+  j.seed = a.seed;
+  j.key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
+  j.sweep = *(volatile uint32_t *)&a.ctl->sweep + (uint32_t)k;
+  j.nspins = a.nspins;
+  j.replica = tix;
+  if (threadIdx.x < 5) thr[threadIdx.x] = a.thr[(int64_t)tix * 5 + threadIdx.x];
+  tile_stage_async<S>(j, stage);
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  j.thr = thr;
+  int changed = tile_sweep_sq4<APP, S>(j, stage);
+  block_count_add(a.nacc_slots, (unsigned long long)changed);
+}
+
+// unlike bonds of every replica in the buffer the sweep k-1 wrote
+template <typename S>
+__global__ void __launch_bounds__(kTileThreads) ensemble_bonds_kernel(EnsArgs a, int k) {
+  const int parity = *(volatile int *)&a.ctl->parity ^ (k & 1);
+  const int t = blockIdx.x;
+  tile_bonds<S>(a, t, a.tile_rep[t], (const S *)(parity ? a.buf1 : a.buf0));
+}
+
+// one block: the exchange round (if `exchange`), then ctl moves on by m sweeps
+__global__ void __launch_bounds__(256) ensemble_advance_kernel(EnsArgs a, int m, int exchange) {
+  EnsCtl *ctl = a.ctl;
+  if (exchange) exchange_round(a, *(volatile uint32_t *)&ctl->xround);
+  if (threadIdx.x == 0) {
+    if (exchange) ctl->xround += 1;
+    ctl->sweep += (uint32_t)m;
+    ctl->parity ^= (m & 1);
+    __threadfence();
   }
 }
 
@@ -297,8 +406,14 @@ struct spkgpu_ensemble {
   int chunk = 10;
   void *kfn = nullptr;
   void *buf[2] = {nullptr, nullptr};
-  int32_t *d_L = nullptr, *d_tile_start = nullptr, *d_tidx = nullptr, *d_group_start = nullptr,
-          *d_slot_t = nullptr, *d_who = nullptr;
+  int2 *d_tile_pos = nullptr;
+  int32_t *d_L = nullptr, *d_tile_start = nullptr, *d_tile_rep = nullptr, *d_tidx = nullptr,
+          *d_group_start = nullptr, *d_slot_t = nullptr, *d_slot_group = nullptr, *d_who = nullptr;
+  unsigned long long *d_nacc_slots = nullptr;
+  int mode = SPKGPU_ENSEMBLE_PERSISTENT;
+  float tune_ms[2] = {-1.0f, -1.0f};  // the autotuner's step times per mode
+  int64_t enq = 0;  // sweeps enqueued so far (the host's copy of ctl->sweep)
+  std::vector<int32_t> slot_init;  // replica in each exchange slot at creation
   int64_t *d_base = nullptr;
   uint64_t *d_thr = nullptr;
   double *d_beta = nullptr;
@@ -313,6 +428,9 @@ struct spkgpu_ensemble {
   int64_t launches = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t kev0 = nullptr, kev1 = nullptr;  // around the sweep kernels of the captured step
+  bool kev_in_graph = false;
+  bool replayed = false;  // a graph replay has been enqueued since the capture
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   EnsArgs args;
@@ -341,6 +459,147 @@ static cudaError_t ens_launch(spkgpu_ensemble *e, int nsweeps) {
   return cudaLaunchCooperativeKernel(e->kfn, dim3(e->grid), dim3(kTileThreads), params, 0, e->stream);
 }
 
+// launch-per-sweep mode: m sweeps, the bonds and exchange round if `exchange`,
+// then the advance of ctl; returns the number of kernels through *nk
+static cudaError_t ens_launch_group(spkgpu_ensemble *e, int m, bool exchange, int64_t *nk) {
+  const EnsArgs &a = e->args;
+  const unsigned nt = (unsigned)e->ntiles;
+  for (int k = 0; k < m; k++) {
+    if (e->d.app == SPKGPU_ISING)
+      ensemble_sweep_kernel<SPKGPU_ISING, int8_t><<<nt, kTileThreads, 0, e->stream>>>(a, k);
+    else
+      ensemble_sweep_kernel<SPKGPU_POTTS, int8_t><<<nt, kTileThreads, 0, e->stream>>>(a, k);
+  }
+  if (exchange) ensemble_bonds_kernel<int8_t><<<nt, kTileThreads, 0, e->stream>>>(a, m);
+  ensemble_advance_kernel<<<1, 256, 0, e->stream>>>(a, m, exchange ? 1 : 0);
+  *nk += m + (exchange ? 1 : 0) + 1;
+  return cudaGetLastError();
+}
+
+// kernels one step (chunk sweeps) launches in the current mode
+static int64_t ens_step_kernels(const spkgpu_ensemble *e) {
+  if (e->mode == SPKGPU_ENSEMBLE_PERSISTENT) return 1;
+  return e->chunk + (e->d.exchange_every > 0 ? 1 : 0) + 1;
+}
+
+// captures one step (chunk sweeps, ending on an exchange point when
+// exchanges are on) in the current mode as e->gexec; leaves e->gexec null if
+// capture is unavailable (steps are then launched directly)
+static void ens_capture(spkgpu_ensemble *e) {
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  e->gexec = nullptr;
+  e->graph = nullptr;
+  cudaStream_t cap = e->stream;
+  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  int64_t nk = 0;
+  // external event nodes around the sweep kernels time them in every replay
+  bool kev = cudaEventRecordWithFlags(e->kev0, cap, cudaEventRecordExternal) == cudaSuccess;
+  cudaError_t le;
+  if (e->mode == SPKGPU_ENSEMBLE_PERSISTENT) {
+    le = ens_launch(e, e->chunk);
+    kev = kev && cudaEventRecordWithFlags(e->kev1, cap, cudaEventRecordExternal) == cudaSuccess;
+  } else {
+    const EnsArgs &a = e->args;
+    const unsigned nt = (unsigned)e->ntiles;
+    for (int k = 0; k < e->chunk; k++) {
+      if (e->d.app == SPKGPU_ISING)
+        ensemble_sweep_kernel<SPKGPU_ISING, int8_t><<<nt, kTileThreads, 0, cap>>>(a, k);
+      else
+        ensemble_sweep_kernel<SPKGPU_POTTS, int8_t><<<nt, kTileThreads, 0, cap>>>(a, k);
+    }
+    kev = kev && cudaEventRecordWithFlags(e->kev1, cap, cudaEventRecordExternal) == cudaSuccess;
+    const bool exchange = e->d.exchange_every > 0;
+    if (exchange) ensemble_bonds_kernel<int8_t><<<nt, kTileThreads, 0, cap>>>(a, e->chunk);
+    ensemble_advance_kernel<<<1, 256, 0, cap>>>(a, e->chunk, exchange ? 1 : 0);
+    le = cudaGetLastError();
+    (void)nk;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(cap, &g);
+  if (le == cudaSuccess && ce == cudaSuccess && g && cudaGraphInstantiate(&e->gexec, g, 0) == cudaSuccess) {
+    e->graph = g;
+    e->kev_in_graph = kev;
+  } else {
+    if (g) cudaGraphDestroy(g);
+    e->gexec = nullptr;
+    e->kev_in_graph = false;
+    cudaGetLastError();
+  }
+  e->replayed = false;
+}
+
+// the mutable device state of a fresh ensemble: zero buffers and counters,
+// every replica at its own temperature
+static cudaError_t ens_reset(spkgpu_ensemble *e) {
+  const int n = e->d.nreplica;
+  std::vector<int32_t> ident(n);
+  std::iota(ident.begin(), ident.end(), 0);
+  std::vector<int32_t> who(n);
+  for (int k = 0; k < n; k++) who[k] = e->slot_init[k];
+  size_t sb = (size_t)e->spin_bytes;
+  cudaMemset(e->buf[0], 0, e->nsites * sb);
+  cudaMemset(e->buf[1], 0, e->nsites * sb);
+  cudaMemset(e->d_bonds, 0, n * 8);
+  cudaMemset(e->d_last_bonds, 0, n * 8);
+  cudaMemset(e->d_ctl, 0, sizeof(EnsCtl));
+  cudaMemset(e->d_nacc_slots, 0, kCounterSlots * sizeof(unsigned long long));
+  cudaMemcpy(e->d_tidx, ident.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_who, who.data(), n * 4, cudaMemcpyHostToDevice);
+  e->parity = 0;
+  e->enq = 0;
+  return cudaDeviceSynchronize();
+}
+
+// Autotuner: times one captured step of each mode on this replica set
+// (after a warm-up step, sites all 1) and keeps the faster; the choice is
+// cached per (app, replicas, tiles, exchange period) for the process.
+// SPKGPU_ENSEMBLE_MODE=persistent|launches forces a mode.
+static int ens_pick_mode(spkgpu_ensemble *e, float *ms_out) {
+  ms_out[0] = ms_out[1] = -1.0f;
+  if (const char *env = getenv("SPKGPU_ENSEMBLE_MODE")) {
+    if (!strcmp(env, "persistent")) return SPKGPU_ENSEMBLE_PERSISTENT;
+    if (!strcmp(env, "launches")) return SPKGPU_ENSEMBLE_LAUNCHES;
+  }
+  static std::mutex mu;
+  static std::map<std::vector<int64_t>, int> cache;
+  std::vector<int64_t> key{e->d.device, e->d.app, e->d.nreplica, e->ntiles, e->d.exchange_every};
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  int best = SPKGPU_ENSEMBLE_PERSISTENT;
+  float best_ms = -1.0f;
+  for (int mode : {SPKGPU_ENSEMBLE_PERSISTENT, SPKGPU_ENSEMBLE_LAUNCHES}) {
+    e->mode = mode;
+    ens_capture(e);
+    if (!e->gexec) continue;
+    cudaMemset(e->buf[0], 1, e->nsites * (size_t)e->spin_bytes);
+    float ms = 0.0f;
+    bool ok = cudaGraphLaunch(e->gexec, e->stream) == cudaSuccess &&
+              cudaEventRecord(e->ev0, e->stream) == cudaSuccess &&
+              cudaGraphLaunch(e->gexec, e->stream) == cudaSuccess &&
+              cudaEventRecord(e->ev1, e->stream) == cudaSuccess && cudaEventSynchronize(e->ev1) == cudaSuccess &&
+              cudaEventElapsedTime(&ms, e->ev0, e->ev1) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      continue;
+    }
+    ms_out[mode] = ms;
+    if (best_ms < 0.0f || ms < best_ms) {
+      best_ms = ms;
+      best = mode;
+    }
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = best;
+  return best;
+}
+
 extern "C" {
 
 const char *spkgpu_ensemble_last_error(const spkgpu_ensemble *e) { return e ? e->err.c_str() : "null handle"; }
@@ -354,9 +613,13 @@ int spkgpu_ensemble_destroy(spkgpu_ensemble *e) {
   cudaFree(e->buf[1]);
   cudaFree(e->d_L);
   cudaFree(e->d_tile_start);
+  cudaFree(e->d_tile_rep);
+  cudaFree(e->d_tile_pos);
+  cudaFree(e->d_nacc_slots);
   cudaFree(e->d_tidx);
   cudaFree(e->d_group_start);
   cudaFree(e->d_slot_t);
+  cudaFree(e->d_slot_group);
   cudaFree(e->d_who);
   cudaFree(e->d_base);
   cudaFree(e->d_thr);
@@ -368,6 +631,8 @@ int spkgpu_ensemble_destroy(spkgpu_ensemble *e) {
   cudaFree(e->d_bad);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->kev0) cudaEventDestroy(e->kev0);
+  if (e->kev1) cudaEventDestroy(e->kev1);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return SPKGPU_OK;
@@ -410,6 +675,16 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   }
   e->nsites = off;
   e->ntiles = tile_start[n];
+  std::vector<int32_t> tile_rep(e->ntiles);
+  std::vector<int2> tile_pos(e->ntiles);
+  for (int r = 0; r < n; r++) {
+    const int tpr = e->L[r] / kTile;
+    for (int t = tile_start[r]; t < tile_start[r + 1]; t++) {
+      const int lt = t - tile_start[r];
+      tile_rep[t] = r;
+      tile_pos[t] = make_int2(r, ((lt / tpr) << 16) | (lt % tpr));
+    }
+  }
   // temperatures: index t = the replica that started with it
   std::vector<uint64_t> thr((size_t)n * 5);
   std::vector<double> beta(n);
@@ -435,10 +710,16 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   }
   group_start.push_back(n);
   e->ngroups = (int)group_start.size() - 1;
+  e->slot_init = who;
+  std::vector<int32_t> slot_group(n);
+  for (int g = 0; g < e->ngroups; g++)
+    for (int k = group_start[g]; k < group_start[g + 1]; k++) slot_group[k] = g;
   std::iota(tidx.begin(), tidx.end(), 0);
 
   if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
-  if (cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
+  if (cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess ||
+      cudaEventCreate(&e->kev0) != cudaSuccess || cudaEventCreate(&e->kev1) != cudaSuccess)
+    return fail(SPKGPU_ERR_CUDA);
   auto dmalloc = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes == 0 ? 16 : bytes) == cudaSuccess; };
   size_t sb = (size_t)e->spin_bytes;
   if (!dmalloc(&e->buf[0], e->nsites * sb) || !dmalloc(&e->buf[1], e->nsites * sb) ||
@@ -448,8 +729,13 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
       !dmalloc((void **)&e->d_base, n * 8) || !dmalloc((void **)&e->d_thr, thr.size() * 8) ||
       !dmalloc((void **)&e->d_beta, n * 8) || !dmalloc((void **)&e->d_bonds, n * 8) ||
       !dmalloc((void **)&e->d_last_bonds, n * 8) || !dmalloc((void **)&e->d_ctl, sizeof(EnsCtl)) ||
-      !dmalloc((void **)&e->d_bad, sizeof(int)))
+      !dmalloc((void **)&e->d_bad, sizeof(int)) || !dmalloc((void **)&e->d_tile_rep, (size_t)e->ntiles * 4) ||
+      !dmalloc((void **)&e->d_nacc_slots, kCounterSlots * sizeof(unsigned long long)) ||
+      !dmalloc((void **)&e->d_slot_group, n * 4) || !dmalloc((void **)&e->d_tile_pos, (size_t)e->ntiles * 8))
     return fail(SPKGPU_ERR_NOMEM);
+  cudaMemcpy(e->d_tile_pos, tile_pos.data(), (size_t)e->ntiles * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_slot_group, slot_group.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_tile_rep, tile_rep.data(), (size_t)e->ntiles * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(e->d_L, e->L.data(), n * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(e->d_tile_start, tile_start.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(e->d_tidx, tidx.data(), n * 4, cudaMemcpyHostToDevice);
@@ -479,6 +765,8 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   a.L = e->d_L;
   a.base = e->d_base;
   a.tile_start = e->d_tile_start;
+  a.tile_rep = e->d_tile_rep;
+  a.tile_pos = e->d_tile_pos;
   a.nrep = n;
   a.ntiles = e->ntiles;
   a.tidx = e->d_tidx;
@@ -486,6 +774,7 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   a.beta = e->d_beta;
   a.group_start = e->d_group_start;
   a.slot_t = e->d_slot_t;
+  a.slot_group = e->d_slot_group;
   a.who = e->d_who;
   a.bonds = e->d_bonds;
   a.last_bonds = e->d_last_bonds;
@@ -495,22 +784,13 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   a.nspins = d.nspins;
   a.seed = d.seed;
   a.ctl = e->d_ctl;
+  a.nacc_slots = e->d_nacc_slots;
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
-  // capture one step (chunk sweeps) as a graph; replayed by spkgpu_ensemble_run
-  cudaStream_t cap = e->stream;
-  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-    cudaError_t le = ens_launch(e, e->chunk);
-    cudaGraph_t g = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(cap, &g);
-    if (le == cudaSuccess && ce == cudaSuccess && g &&
-        cudaGraphInstantiate(&e->gexec, g, 0) == cudaSuccess) {
-      e->graph = g;
-    } else {
-      if (g) cudaGraphDestroy(g);
-      e->gexec = nullptr;
-      cudaGetLastError();  // capture unsupported: launch directly instead
-    }
-  }
+  // pick the faster execution form for this replica set, then start from a
+  // clean state and capture one step of it as a graph
+  e->mode = ens_pick_mode(e, e->tune_ms);
+  if (ens_reset(e) != cudaSuccess) return fail(ens_cuda(e, cudaGetLastError(), "ensemble reset"));
+  ens_capture(e);
   *out = e;
   return SPKGPU_OK;
 }
@@ -552,18 +832,37 @@ int spkgpu_ensemble_download(spkgpu_ensemble *e, int32_t *spin, int64_t n) {
 
 static int ens_enqueue(spkgpu_ensemble *e, int32_t nsweeps) {
   int32_t left = nsweeps;
+  const int every = e->d.exchange_every;
   while (left > 0) {
-    if (e->gexec && left >= e->chunk) {
-      ENS_CUDA(e, cudaGraphLaunch(e->gexec, e->stream));
-      left -= e->chunk;
-      e->parity ^= (e->chunk & 1);
+    int32_t m;
+    if (e->mode == SPKGPU_ENSEMBLE_PERSISTENT) {
+      // the kernel places exchanges itself (after every sweep whose count is
+      // a multiple of the period)
+      m = std::min(left, e->chunk);
+      if (e->gexec && m == e->chunk) {
+        ENS_CUDA(e, cudaGraphLaunch(e->gexec, e->stream));
+        e->replayed = true;
+      } else {
+        ENS_CUDA(e, ens_launch(e, m));
+      }
+      e->launches++;
     } else {
-      int32_t m = std::min(left, e->chunk);
-      ENS_CUDA(e, ens_launch(e, m));
-      left -= m;
-      e->parity ^= (m & 1);
+      // groups end at exchange points; a whole period from one is the graph
+      const int32_t pos = every > 0 ? (int32_t)(e->enq % every) : 0;
+      const int32_t room = every > 0 ? every - pos : e->chunk;
+      m = std::min(left, room);
+      if (e->gexec && pos == 0 && m == e->chunk) {
+        ENS_CUDA(e, cudaGraphLaunch(e->gexec, e->stream));
+        e->replayed = true;
+        e->launches += ens_step_kernels(e);
+      } else {
+        const bool exchange = every > 0 && (e->enq + m) % every == 0;
+        ENS_CUDA(e, ens_launch_group(e, m, exchange, &e->launches));
+      }
     }
-    e->launches++;
+    left -= m;
+    e->enq += m;
+    e->parity ^= (m & 1);
   }
   e->nsweeps_done += nsweeps;
   return SPKGPU_OK;
@@ -600,7 +899,11 @@ int spkgpu_ensemble_get_stats(spkgpu_ensemble *e, spkgpu_ensemble_stats *out) {
   if (rc) return rc;
   EnsCtl c;
   ENS_CUDA(e, cudaMemcpy(&c, e->d_ctl, sizeof(c), cudaMemcpyDeviceToHost));
-  out->naccept = (int64_t)c.naccept;
+  unsigned long long slots[kCounterSlots];
+  ENS_CUDA(e, cudaMemcpy(slots, e->d_nacc_slots, sizeof(slots), cudaMemcpyDeviceToHost));
+  unsigned long long nacc = c.naccept;
+  for (int k = 0; k < kCounterSlots; k++) nacc += slots[k];
+  out->naccept = (int64_t)nacc;
   out->nattempt = e->nsites * e->nsweeps_done;
   out->nsweeps = e->nsweeps_done;
   out->exchange_tries = (int64_t)c.xtries;
@@ -623,6 +926,26 @@ int spkgpu_ensemble_energies(spkgpu_ensemble *e, int64_t *bonds) {
   int rc = spkgpu_ensemble_synchronize(e);
   if (rc) return rc;
   ENS_CUDA(e, cudaMemcpy(bonds, e->d_last_bonds, (size_t)e->d.nreplica * 8, cudaMemcpyDeviceToHost));
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_sweep_kernel_ms(spkgpu_ensemble *e, float *ms, int32_t *nlaunch) {
+  if (!e || !ms || !nlaunch) return SPKGPU_ERR_ARG;
+  if (!e->kev_in_graph || !e->replayed)
+    return ens_fail(e, SPKGPU_ERR_UNSUPPORTED, "no replay of a captured step to time");
+  ENS_CUDA(e, cudaEventSynchronize(e->kev1));
+  ENS_CUDA(e, cudaEventElapsedTime(ms, e->kev0, e->kev1));
+  *nlaunch = (e->mode == SPKGPU_ENSEMBLE_PERSISTENT) ? 1 : e->chunk;
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_mode(const spkgpu_ensemble *e, int32_t *mode, float *tune_ms) {
+  if (!e || !mode) return SPKGPU_ERR_ARG;
+  *mode = e->mode;
+  if (tune_ms) {
+    tune_ms[0] = e->tune_ms[0];
+    tune_ms[1] = e->tune_ms[1];
+  }
   return SPKGPU_OK;
 }
 

@@ -202,9 +202,17 @@ constexpr int kSegPerThread = kTile * kTile / 8 / kTileThreads;  // 8-site segme
 static_assert(kSegPerThread * 4 == kPairsPerThread, "a segment holds four x-pairs");
 static_assert(kSegPerThread * 8 * kTileThreads == kTile * kTile, "segments must cover the tile");
 
-// lane code of one site from its two draws
+// lane code of one site from its two draws; T32: both thresholds are below
+// 2^32 (every finite temperature whose exp(-2/T) rounds below 1), so the
+// tests are 32-bit compares
+template <bool T32>
 __device__ __forceinline__ uint32_t ising_lane_code(uint32_t x0, uint32_t x1, uint64_t t2, uint64_t t4) {
-  return (uint32_t)((uint64_t)x1 < t4) + (uint32_t)((uint64_t)x1 < t2) + (x0 < 0x7FFFFFFFu ? 4u : 0u);
+  uint32_t lvl;
+  if (T32)
+    lvl = (uint32_t)(x1 < (uint32_t)t4) + (uint32_t)(x1 < (uint32_t)t2);
+  else
+    lvl = (uint32_t)((uint64_t)x1 < t4) + (uint32_t)((uint64_t)x1 < t2);
+  return lvl + (x0 < 0x7FFFFFFFu ? 4u : 0u);
 }
 
 // unlike-neighbour counts of the eight lanes of the segment at stage index c
@@ -227,7 +235,7 @@ __device__ __forceinline__ uint64_t seg_flips(uint64_t e, uint64_t v, uint64_t l
   return (p ^ v) & acc & cmask;
 }
 
-template <typename S>
+template <typename S, bool T32>
 __device__ __forceinline__ int tile_segments_ising8(const TileJob &j, S *stage_s) {
   static_assert(sizeof(S) == 1, "byte lanes");
   int8_t *stage = (int8_t *)stage_s;
@@ -248,7 +256,7 @@ __device__ __forceinline__ int tile_segments_ising8(const TileJob &j, S *stage_s
     for (int i = 0; i < 4; i++) {
       const int64_t pr = (s >> 1) + i;
       U4 w = philox4x32_10_rk(U4{(uint32_t)pr, (uint32_t)(pr >> 32), j.sweep, 0u}, rk);
-      uint32_t c2 = ising_lane_code(w.x, w.y, t2, t4) | (ising_lane_code(w.z, w.w, t2, t4) << 8);
+      uint32_t c2 = ising_lane_code<T32>(w.x, w.y, t2, t4) | (ising_lane_code<T32>(w.z, w.w, t2, t4) << 8);
       code |= (uint64_t)c2 << (16 * i);
     }
     lv[k] = code;
@@ -292,9 +300,11 @@ __device__ __forceinline__ int tile_segments_ising8(const TileJob &j, S *stage_s
 // Returns the number of site values changed inside the tile.
 template <int APP, typename S>
 __device__ __forceinline__ int tile_sweep_sq4(const TileJob &j, S *stage) {
-  if constexpr (APP == SPKGPU_ISING && sizeof(S) == 1)
-    return tile_segments_ising8<S>(j, stage);
-  else
+  if constexpr (APP == SPKGPU_ISING && sizeof(S) == 1) {
+    // thr[2] >= thr[4]: one test covers both (uniform across the block)
+    if ((j.thr[2] >> 32) == 0) return tile_segments_ising8<S, true>(j, stage);
+    return tile_segments_ising8<S, false>(j, stage);
+  } else
     return tile_pairs_sq4<APP, S>(j, stage);
 }
 

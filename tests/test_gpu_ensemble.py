@@ -49,11 +49,20 @@ def ensemble_case(seed=777):
     return L, T, spins
 
 
-@pytest.mark.parametrize("every,nsweeps,chunks", [(0, 7, [3, 4]), (2, 8, [2, 6]), (3, 12, [12]), (1, 5, [2, 3])])
-def test_ensemble_matches_oracle(sg, every, nsweeps, chunks):
+@pytest.fixture(params=["persistent", "launches"])
+def mode(request, monkeypatch):
+    """both execution forms of the ensemble, forced past the autotuner"""
+    monkeypatch.setenv("SPKGPU_ENSEMBLE_MODE", request.param)
+    return request.param
+
+
+@pytest.mark.parametrize("every,nsweeps,chunks", [(0, 7, [3, 4]), (2, 8, [2, 6]), (3, 12, [12]), (1, 5, [2, 3]),
+                                                  (4, 13, [3, 2, 8])])
+def test_ensemble_matches_oracle(sg, mode, every, nsweeps, chunks):
     L, T, spins = ensemble_case()
     seed = 99
     ens = sg.Ensemble(L, T, "ising", 2, seed=seed, exchange_every=every)
+    assert ens.mode()["mode"] == mode
     ens.upload(np.concatenate(spins))
     ref = [s.copy() for s in spins]
     orc = oracle.EnsembleOracle(L, T, "ising", 2, seed=seed, every=every)
@@ -72,7 +81,7 @@ def test_ensemble_matches_oracle(sg, every, nsweeps, chunks):
         assert ens.energies().tolist() == orc.last_bonds
 
 
-def test_ensemble_potts(sg):
+def test_ensemble_potts(sg, mode):
     L = [32, 64, 64]
     T = [0.6, 0.9, 0.8]
     spins = [oracle.init_spins(5 + r, l * l, 1, 12) for r, l in enumerate(L)]
@@ -86,6 +95,18 @@ def test_ensemble_potts(sg):
     for r in range(3):
         assert np.array_equal(ens.replica(got, r), ref[r])
     assert ens.temperatures().tolist() == orc.temperatures()
+    assert ens.stats()["naccept"] == orc.naccept
+
+
+def test_autotuner_times_both_forms_then_caches(sg, monkeypatch):
+    monkeypatch.delenv("SPKGPU_ENSEMBLE_MODE", raising=False)
+    L, T = [64, 96, 32, 64, 32], [1.8, 2.2, 2.6, 3.0, 3.4]  # a replica set no other test uses
+    first = sg.Ensemble(L, T, "ising", 2, seed=1, exchange_every=5).mode()
+    assert first["mode"] in ("persistent", "launches")
+    assert all(v is not None and v > 0 for v in first["tune_ms"].values())
+    again = sg.Ensemble(L, T, "ising", 2, seed=2, exchange_every=5).mode()
+    assert again["mode"] == first["mode"]
+    assert all(v is None for v in again["tune_ms"].values())  # cached: nothing timed
 
 
 def test_ensemble_rejects_bad_sizes(sg):
