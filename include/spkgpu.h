@@ -125,6 +125,16 @@ int spkgpu_set_sweep_index(spkgpu_lattice *h, int64_t sweep);
 int spkgpu_get_stats(spkgpu_lattice *h, spkgpu_stats *out);
 /* total energy = sum of site energies (waits for the stream) */
 int spkgpu_energy(spkgpu_lattice *h, double *energy);
+/* sum, minimum and maximum of the site values (vmin, vmax may be NULL):
+   `diag_style array i1 mean|sum|min|max` (src/diag_array.cpp:107-200; mean
+   = sum / nsites); the Ising magnetisation is 2 * mean - 3 */
+int spkgpu_site_stats(spkgpu_lattice *h, int64_t *sum, int32_t *vmin, int32_t *vmax);
+/* `diag_style cluster` (src/diag_cluster.cpp:229-609): connected components
+   of equal site values over the lattice neighbours with periodic wrap;
+   ncluster = Nclust, mean_volume = <N>, mean_radius = <R> (mean of
+   volume^(1/dimension)).  At most 2^31-1 sites; allocates 8 bytes per site
+   of scratch on first use, kept until spkgpu_destroy. */
+int spkgpu_clusters(spkgpu_lattice *h, int64_t *ncluster, double *mean_volume, double *mean_radius);
 int spkgpu_synchronize(spkgpu_lattice *h);
 /* enqueue nsweeps sweeps bracketed by CUDA events on the handle's stream,
    wait, and report the elapsed device time in milliseconds */

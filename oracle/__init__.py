@@ -97,6 +97,8 @@ def lib():
         L.spko_sector.argtypes = [P(Cfg), ctypes.c_int64]
         L.spko_energy.argtypes = [P(Cfg), i32p]
         L.spko_energy.restype = ctypes.c_double
+        L.spko_clusters.argtypes = [P(Cfg), i32p, P(ctypes.c_int64), P(ctypes.c_double), P(ctypes.c_double)]
+        L.spko_clusters.restype = ctypes.c_int
         L.spko_hash.argtypes = [i32p, ctypes.c_int64]
         L.spko_hash.restype = ctypes.c_uint64
         L.spko_init_spins.argtypes = [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int, ctypes.c_int, i32p]
@@ -180,6 +182,17 @@ def color_sweeps(cfg: Cfg, spin: np.ndarray, sweep0: int, nsweeps: int, siteseed
 
 def energy(cfg: Cfg, spin: np.ndarray) -> float:
     return lib().spko_energy(ctypes.byref(cfg), _ptr(spin, ctypes.c_int32))
+
+
+def clusters(cfg: Cfg, spin: np.ndarray) -> dict:
+    """diag_style cluster of one lattice: Nclust, <N>, <R>."""
+    s = np.ascontiguousarray(spin, dtype=np.int32)
+    nc, vav, rav = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+    rc = lib().spko_clusters(ctypes.byref(cfg), _ptr(s, ctypes.c_int32), ctypes.byref(nc), ctypes.byref(vav),
+                             ctypes.byref(rav))
+    if rc != 0:
+        raise MemoryError("spko_clusters")
+    return {"ncluster": nc.value, "mean_volume": vav.value, "mean_radius": rav.value}
 
 
 def spin_hash(spin: np.ndarray) -> int:

@@ -516,6 +516,58 @@ double spko_energy(const spko_cfg *c, const int32_t *spin) {
   return e;
 }
 
+/* Cluster analysis of `diag_style cluster` on one process: sites are taken
+   in index order, each unvisited site starts a cluster that grows through
+   equal-valued neighbours (DiagCluster::generate_clusters,
+   src/diag_cluster.cpp:229-360; AppLattice::push_connected_neighbors,
+   src/app_lattice.cpp:1187-1201); with periodic wrap the pieces the
+   reference joins across the boundary (src/diag_cluster.cpp:480-597) are
+   one component here.  Volumes and volume^(1/dim) are summed in cluster
+   order, as the reference does (src/diag_cluster.cpp:597-605). */
+int spko_clusters(const spko_cfg *c, const int32_t *spin, int64_t *ncluster, double *vav, double *rav) {
+  int64_t n = nsites(c);
+  int32_t *seen = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+  int64_t *stack = (int64_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  if (!seen || !stack) {
+    free(seen);
+    free(stack);
+    return -1;
+  }
+  int dim = is2d(c) ? 2 : 3;
+  double invdim = 1.0 / dim;
+  double volsum = 0.0, rsum = 0.0;
+  int64_t nc = 0;
+  int64_t nb[26];
+  for (int64_t i = 0; i < n; i++) {
+    if (seen[i]) continue;
+    nc++;
+    int64_t top = 0;
+    stack[top++] = i;
+    seen[i] = 1;
+    double vol = 0.0;
+    while (top > 0) {
+      int64_t ii = stack[--top];
+      vol += 1.0;
+      int nn = spko_neighbors(c, ii, nb);
+      for (int j = 0; j < nn; j++) {
+        int64_t m = nb[j];
+        if (spin[m] == spin[ii] && !seen[m]) {
+          seen[m] = 1;
+          stack[top++] = m;
+        }
+      }
+    }
+    volsum += vol;
+    rsum += pow(vol, invdim);
+  }
+  free(seen);
+  free(stack);
+  *ncluster = nc;
+  *vav = nc ? volsum / (double)nc : 0.0;
+  *rav = nc ? rsum / (double)nc : 0.0;
+  return 0;
+}
+
 /* ---------------------------------------------------------------------- */
 /* KMC with the tree solver over sectors                                  */
 /* ---------------------------------------------------------------------- */

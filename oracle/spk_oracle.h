@@ -40,6 +40,7 @@ int spko_neighbors(const spko_cfg *c, int64_t i, int64_t *out);
 int spko_color(const spko_cfg *c, int64_t i);
 int spko_sector(const spko_cfg *c, int64_t i);
 double spko_energy(const spko_cfg *c, const int32_t *spin);
+int spko_clusters(const spko_cfg *c, const int32_t *spin, int64_t *ncluster, double *vav, double *rav);
 uint64_t spko_hash(const int32_t *spin, int64_t n);
 void spko_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 void spko_init_spins(uint32_t seed, int64_t n, int lo, int hi, int32_t *spin);

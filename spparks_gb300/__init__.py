@@ -94,7 +94,7 @@ EXPORTS = [
     "spkgpu_create", "spkgpu_destroy", "spkgpu_last_error", "spkgpu_version", "spkgpu_set_temperature",
     "spkgpu_upload_spins", "spkgpu_download_spins", "spkgpu_init_spins", "spkgpu_upload_siteseeds", "spkgpu_download_siteseeds",
     "spkgpu_upload_mask", "spkgpu_download_mask", "spkgpu_sweep", "spkgpu_set_sweep_index",
-    "spkgpu_get_stats", "spkgpu_energy", "spkgpu_synchronize", "spkgpu_timed_sweeps", "spkgpu_stream",
+    "spkgpu_get_stats", "spkgpu_energy", "spkgpu_site_stats", "spkgpu_clusters", "spkgpu_synchronize", "spkgpu_timed_sweeps", "spkgpu_stream",
     "spkgpu_device_spins", "spkgpu_launch_count", "spkgpu_kmc_setup", "spkgpu_kmc_run",
     "spkgpu_ensemble_create", "spkgpu_ensemble_destroy", "spkgpu_ensemble_last_error", "spkgpu_ensemble_upload",
     "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
@@ -134,6 +134,8 @@ def load_library(path: Path | None = None):
     L.spkgpu_set_sweep_index.argtypes = [vp, ctypes.c_int64]
     L.spkgpu_get_stats.argtypes = [vp, P(Stats)]
     L.spkgpu_energy.argtypes = [vp, P(ctypes.c_double)]
+    L.spkgpu_site_stats.argtypes = [vp, P(ctypes.c_int64), P(ctypes.c_int32), P(ctypes.c_int32)]
+    L.spkgpu_clusters.argtypes = [vp, P(ctypes.c_int64), P(ctypes.c_double), P(ctypes.c_double)]
     L.spkgpu_synchronize.argtypes = [vp]
     L.spkgpu_timed_sweeps.argtypes = [vp, ctypes.c_int32, P(ctypes.c_float)]
     L.spkgpu_stream.argtypes = [vp, P(vp)]
@@ -266,6 +268,18 @@ class Lattice:
         e = ctypes.c_double()
         self._check(self.lib.spkgpu_energy(self.h, ctypes.byref(e)))
         return e.value
+
+    def site_stats(self) -> dict:
+        """sum, min, max and mean of the site values (diag_style array i1)."""
+        s, lo, hi = ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.spkgpu_site_stats(self.h, ctypes.byref(s), ctypes.byref(lo), ctypes.byref(hi)))
+        return {"sum": s.value, "min": lo.value, "max": hi.value, "mean": s.value / self.n}
+
+    def clusters(self) -> dict:
+        """diag_style cluster: number of clusters, <N> and <R>."""
+        nc, vav, rav = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.spkgpu_clusters(self.h, ctypes.byref(nc), ctypes.byref(vav), ctypes.byref(rav)))
+        return {"ncluster": nc.value, "mean_volume": vav.value, "mean_radius": rav.value}
 
     def synchronize(self):
         self._check(self.lib.spkgpu_synchronize(self.h))

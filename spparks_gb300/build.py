@@ -28,6 +28,7 @@ SOURCES = [
     "noalloc.cu",
     "packed.cu",
     "sweep_rows.cu",
+    "diag.cu",
     "driver.cpp",
 ]
 

@@ -12,10 +12,15 @@
 //   set site range LO HI | set site value V   (Set::command, src/set.cpp)
 //   sweep color | color/strict [mask yes|no]   (AppLattice::set_sweep)
 //   sector yes|no|2|4|8 [nstop N | tstop T]     (AppLattice::set_sector)
-//   temperature T, solve_style tree | none, stats DT, diag_style energy
+//   temperature T, solve_style tree | none, stats DT
+//   diag_style energy | array i1 mean|sum|min|max ... | cluster
+//                                   stats columns of DiagEnergy, DiagArray,
+//                                   DiagCluster (src/diag_*.cpp), computed on
+//                                   the device (spkgpu_energy/site_stats/
+//                                   clusters)
 //   run DT [upto] [pre yes|no] [post yes|no]    (App::run, src/app.cpp:86-148)
-// Output-only commands (dump, diag_style cluster, ...) are accepted and
-// ignored with a warning.  `sweep random|raster` (serial by definition) is
+// Output-only commands (dump, the cluster diagnostic's files, ...) are
+// accepted and ignored with a warning.  `sweep random|raster` (serial by definition) is
 // refused.  Errors are printed as "ERROR: ..." like Error::all, but the
 // process is not terminated: the command returns NULL and the message stays
 // readable through spkgpu_driver_error().
@@ -148,7 +153,15 @@ struct Driver {
   double temperature = 0.0;
   bool tree = false;
   double stats_delta = 0.0;
-  bool diag_energy = false;
+  // diagnostics in declaration order (Output::stats_header prints them so)
+  enum { DIAG_ENERGY, DIAG_ARRAY, DIAG_CLUSTER };
+  enum { AMEAN, ASUM, AMIN, AMAX };
+  struct DiagSpec {
+    int kind;
+    bool stats = true;
+    std::vector<int> methods;  // array: one column per (i1, method) pair
+  };
+  std::vector<DiagSpec> diags;
   // run state
   double time = 0.0;
   int64_t nsweeps = 0, naccept = 0, nattempt = 0;
@@ -208,6 +221,9 @@ struct Driver {
 
   bool command(std::vector<std::string> &w);
   bool run(std::vector<std::string> &w);
+  bool diag_style(std::vector<std::string> &w);
+  std::string diag_header() const;
+  std::string diag_values();
   bool ensure_handle();
   bool sync_to_host();
   void stats_line(double cpu);
@@ -286,11 +302,129 @@ void Driver::stats_line(double cpu) {
   char line[256];
   int off = snprintf(line, sizeof(line), "%10g %10lld %10lld %10lld %10.3g", time, (long long)naccept,
                      (long long)(tree ? 0 : nattempt - naccept), (long long)nsweeps, cpu);
-  if (diag_energy && h) {
-    double e = 0.0;
-    if (spkgpu_energy(h, &e) == 0) snprintf(line + off, sizeof(line) - off, " %10g", e);
+  std::string out = line;
+  if (h) out += diag_values();
+  print("%s\n", out.c_str());
+}
+
+// Diag::Diag (src/diag.cpp:40-98) keywords, then the style's own:
+// DiagArray takes (iN|dN, mean|sum|min|max) pairs only
+// (src/diag_array.cpp:36-90), DiagCluster filename/dump/site/size
+// (src/diag_cluster.cpp:60-110; their files are not written here)
+bool Driver::diag_style(std::vector<std::string> &w) {
+  if (app_id < 0) return fail("Diag_style command before app_style set");
+  if (w.size() < 2) return fail("Illegal diag_style command");
+  DiagSpec d;
+  size_t k = 2;
+  auto base_keywords = [&]() -> bool {
+    while (k < w.size()) {
+      if (w[k] == "stats") {
+        if (k + 1 >= w.size() || (w[k + 1] != "yes" && w[k + 1] != "no")) return fail("Illegal diag_style command");
+        d.stats = w[k + 1] == "yes";
+        k += 2;
+      } else if (w[k] == "delt" || w[k] == "delay") {
+        if (k + 1 >= w.size()) return fail("Illegal diag_style command");
+        print("WARNING: diag_style %s is ignored by the GPU driver\n", w[k].c_str());
+        k += 2;
+      } else if (w[k] == "logfreq" || w[k] == "loglinfreq") {
+        if (k + 2 >= w.size()) return fail("Illegal diag_style command");
+        print("WARNING: diag_style %s is ignored by the GPU driver\n", w[k].c_str());
+        k += 3;
+      } else {
+        break;
+      }
+    }
+    return true;
+  };
+  if (w[1] == "energy") {
+    d.kind = DIAG_ENERGY;
+    if (!base_keywords()) return false;
+    if (k < w.size()) return fail("Illegal diag_style command");
+  } else if (w[1] == "array") {
+    d.kind = DIAG_ARRAY;
+    if ((w.size() - 2) % 2 != 0 || w.size() < 4) return fail("Invalid diag_style command");
+    for (k = 2; k < w.size(); k += 2) {
+      // the on-lattice apps of this path have one integer array (the site
+      // values) and no double arrays
+      if (w[k] != "i1") return fail("Invalid diag_style command");
+      const std::string &m = w[k + 1];
+      if (m == "mean") d.methods.push_back(AMEAN);
+      else if (m == "sum") d.methods.push_back(ASUM);
+      else if (m == "min") d.methods.push_back(AMIN);
+      else if (m == "max") d.methods.push_back(AMAX);
+      else return fail("Invalid diag_style command");
+    }
+  } else if (w[1] == "cluster") {
+    d.kind = DIAG_CLUSTER;
+    if (!base_keywords()) return false;
+    while (k < w.size()) {
+      if (w[k] == "filename" && k + 1 < w.size()) k += 2;
+      else if (w[k] == "dump" && k + 1 < w.size()) k += (w[k + 1] == "none") ? 2 : 3;
+      else if (w[k] == "site/size") k += 1;
+      else return fail("Illegal diag_style cluster command");
+      print("WARNING: diag_style cluster output files are not written by the GPU driver\n");
+    }
+  } else {
+    print("WARNING: diag_style %s is ignored by the GPU driver\n", w[1].c_str());
+    return true;
   }
-  print("%s\n", line);
+  diags.push_back(d);
+  return true;
+}
+
+std::string Driver::diag_header() const {
+  static const char *names[] = {"mean", "sum", "min", "max"};
+  std::string out;
+  char buf[64];
+  for (const DiagSpec &d : diags) {
+    if (!d.stats) continue;
+    if (d.kind == DIAG_ENERGY) {
+      snprintf(buf, sizeof(buf), " %10s", "Energy");
+      out += buf;
+    } else if (d.kind == DIAG_ARRAY) {
+      for (int m : d.methods) {
+        std::string col = std::string(names[m]) + "(i1)";
+        snprintf(buf, sizeof(buf), " %10s", col.c_str());
+        out += buf;
+      }
+    } else {
+      snprintf(buf, sizeof(buf), " %10s %10s %10s", "Nclust", "<N>", "<R>");
+      out += buf;
+    }
+  }
+  return out;
+}
+
+// the diag columns of one stats line, from the device lattice
+std::string Driver::diag_values() {
+  std::string out;
+  char buf[96];
+  for (const DiagSpec &d : diags) {
+    if (!d.stats) continue;
+    if (d.kind == DIAG_ENERGY) {
+      double e = 0.0;
+      if (spkgpu_energy(h, &e) != 0) continue;
+      snprintf(buf, sizeof(buf), " %10g", e);
+      out += buf;
+    } else if (d.kind == DIAG_ARRAY) {
+      int64_t sum = 0;
+      int32_t lo = 0, hi = 0;
+      if (spkgpu_site_stats(h, &sum, &lo, &hi) != 0) continue;
+      for (int m : d.methods) {
+        double v = m == AMEAN ? (double)sum / (double)n()
+                              : m == ASUM ? (double)sum : m == AMIN ? (double)lo : (double)hi;
+        snprintf(buf, sizeof(buf), " %10g", v);
+        out += buf;
+      }
+    } else {
+      int64_t nc = 0;
+      double vav = 0.0, rav = 0.0;
+      if (spkgpu_clusters(h, &nc, &vav, &rav) != 0) continue;
+      snprintf(buf, sizeof(buf), " %10d %10g %10g", (int)nc, vav, rav);
+      out += buf;
+    }
+  }
+  return out;
 }
 
 bool Driver::run(std::vector<std::string> &w) {
@@ -342,8 +476,7 @@ bool Driver::run(std::vector<std::string> &w) {
   host_valid = false;
   first_run = false;
   print("Setting up run ...\n");
-  print("%10s %10s %10s %10s %10s%s\n", "Time", "Naccept", "Nreject", "Nsweeps", "CPU",
-        diag_energy ? "     Energy" : "");
+  print("%10s %10s %10s %10s %10s%s\n", "Time", "Naccept", "Nreject", "Nsweeps", "CPU", diag_header().c_str());
   double t0 = wall();
   stats_line(0.0);
   double nextoutput = stats_delta > 0.0 ? time + stats_delta : stoptime;
@@ -536,8 +669,7 @@ bool Driver::command(std::vector<std::string> &w) {
   } else if (c == "stats") {
     if (!need(2) || !parse_double(w[1], &stats_delta)) return fail("Illegal stats command");
   } else if (c == "diag_style") {
-    if (need(2) && w[1] == "energy") diag_energy = true;
-    else print("WARNING: diag_style %s is ignored by the GPU driver\n", need(2) ? w[1].c_str() : "");
+    return diag_style(w);
   } else if (c == "run") {
     return run(w);
   } else if (c == "dump" || c == "undump" || c == "dump_modify" || c == "echo" || c == "log" ||

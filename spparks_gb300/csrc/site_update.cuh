@@ -50,6 +50,19 @@ struct Stencil {
   }
 };
 
+// linear index of the periodic neighbour (x+dx, y+dy, z+dz) (site index =
+// id-1 = x + nx*(y + ny*z), src/create_sites.cpp:506-655)
+template <int LAT>
+__device__ __forceinline__ int64_t wrap_index(int x, int y, int z, int dx, int dy, int dz, int nx, int ny,
+                                              int nz) {
+  int xn = x + dx, yn = y + dy, zn = z + dz;
+  xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
+  yn = yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn);
+  if (Stencil<LAT>::k3d) zn = zn < 0 ? zn + nz : (zn >= nz ? zn - nz : zn);
+  else zn = 0;
+  return (int64_t)xn + (int64_t)nx * ((int64_t)yn + (int64_t)ny * zn);
+}
+
 // bit j set <=> neighbour j holds a value that differs from `own` and from
 // every earlier neighbour: the reference's unique[] list in order
 template <int NN>

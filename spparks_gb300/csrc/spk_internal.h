@@ -161,7 +161,8 @@ struct spkgpu_lattice {
   bool packed = false;          // spin_bytes == -1: 64 Ising sites per uint64
   int32_t *d_seeds = nullptr;
   uint8_t *d_mask = nullptr;
-  unsigned long long *d_counters = nullptr;  // [0] naccept, [1] energy, [2] flags
+  unsigned long long *d_counters = nullptr;  // [1] energy, [2] bad-value flag, [3..5] diagnostics
+  int32_t *d_labels = nullptr;  // diagnostics: cluster labels and sizes (2n int32) + partial sums
   int32_t *d_stage = nullptr;   // int32 staging for upload/download
   int64_t stage_n = 0;
   int32_t *d_axis = nullptr;    // per-axis coordinate lists and tables

@@ -24,7 +24,8 @@
 
 using spk::AcceptTable;
 
-// d_counters layout: [0,8) scalars ([1] energy, [2] bad-value flag),
+// d_counters layout: [0,8) scalars ([1] energy, [2] bad-value flag, [3..5]
+// site diagnostics),
 // [8, 8+256) Naccept slots
 static const int kNacceptSlots = 8;
 static const int kCounterWords = kNacceptSlots + spk::kCounterSlots;
@@ -259,6 +260,7 @@ int spkgpu_destroy(spkgpu_lattice *h) {
   cudaFree(h->d_seeds);
   cudaFree(h->d_mask);
   cudaFree(h->d_counters);
+  cudaFree(h->d_labels);
   cudaFree(h->d_stage);
   cudaFree(h->d_axis);
   if (h->ev0) cudaEventDestroy(h->ev0);

@@ -22,17 +22,6 @@
 
 namespace spk {
 
-template <int LAT>
-__device__ __forceinline__ int64_t wrap_index(int x, int y, int z, int dx, int dy, int dz, int nx, int ny,
-                                              int nz) {
-  int xn = x + dx, yn = y + dy, zn = z + dz;
-  xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
-  yn = yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn);
-  if (Stencil<LAT>::k3d) zn = zn < 0 ? zn + nz : (zn >= nz ? zn - nz : zn);
-  else zn = 0;
-  return (int64_t)xn + (int64_t)nx * ((int64_t)yn + (int64_t)ny * zn);
-}
-
 template <typename S, int LAT, int APP>
 __global__ void __launch_bounds__(256) phase_kernel(PhaseArgs a) {
   constexpr int NN = Stencil<LAT>::NN;

@@ -182,6 +182,48 @@ LOG_CASES = [
 ]
 
 
+# unmodified reference runs with the site diagnostics: the t = 0 row pins the
+# oracle's cluster analysis on the initial `set site range` lattice, every
+# row pins the GPU driver's diag columns
+DIAG_LOG_CASES = [
+    dict(name="diag_strict_potts_sq8n_32", lines=[
+        "seed 2468", "app_style potts 10", "dimension 2", "lattice sq/8n 1.0", "region box block 0 32 0 32 -0.5 0.5",
+        "create_box box", "create_sites box", "set site range 1 10", "sweep color/strict", "diag_style energy",
+        "diag_style array i1 mean i1 max", "diag_style cluster", "temperature 0.4", "stats 2.0", "run 10.0"]),
+    dict(name="diag_strict_ising_sc6n_12", lines=[
+        "seed 97531", "app_style ising", "dimension 3", "lattice sc/6n 1.0", "region box block 0 12 0 12 0 12",
+        "create_box box", "create_sites box", "set site range 1 2", "sweep color/strict", "diag_style energy",
+        "diag_style cluster", "diag_style array i1 mean", "temperature 3.0", "stats 1.0", "run 4.0"]),
+    dict(name="diag_strict_ising_sq4n_40", lines=[
+        "seed 1357", "app_style ising", "dimension 2", "lattice sq/4n 1.0", "region box block 0 40 0 40 -0.5 0.5",
+        "create_box box", "create_sites box", "set site range 1 2", "sweep color/strict", "diag_style cluster",
+        "diag_style array i1 sum i1 min", "temperature 1.5", "stats 5.0", "run 20.0"]),
+]
+
+
+def spk_serial_table(binary, lines):
+    """Header tokens and the stats rows (as printed tokens) of a reference run."""
+    with tempfile.TemporaryDirectory(dir=str(ROOT / "oracle" / "_ref")) as d:
+        inp = Path(d) / "in.case"
+        inp.write_text("\n".join(lines) + "\n")
+        subprocess.run([str(binary), "-in", "in.case", "-screen", "none", "-log", "log.case"], cwd=d, check=True,
+                       capture_output=True)
+        text = (Path(d) / "log.case").read_text().splitlines()
+    header, rows = None, []
+    for line in text:
+        p = line.split()
+        if p[:4] == ["Time", "Naccept", "Nreject", "Nsweeps"]:
+            header = p
+            continue
+        if header is not None:
+            if len(p) == len(header) and p[0][0].isdigit():
+                rows.append(p)
+                continue
+            if rows:
+                break
+    return header, rows
+
+
 def spk_serial_stats(binary, lines):
     """Stats rows (Time Naccept Nreject Nsweeps Energy) printed by the reference."""
     with tempfile.TemporaryDirectory(dir=str(ROOT / "oracle" / "_ref")) as d:
@@ -255,6 +297,11 @@ def main():
         rows = spk_serial_stats(serial, case["lines"])
         fixtures["logs"].append({"case": case, "rows": rows})
         print("log case", case["name"], len(rows), "rows")
+    fixtures["diag_logs"] = []
+    for case in DIAG_LOG_CASES:
+        header, rows = spk_serial_table(serial, case["lines"])
+        fixtures["diag_logs"].append({"case": case, "header": header, "rows": rows})
+        print("diag log case", case["name"], header, len(rows), "rows")
     (HERE / "reference_philox.json").write_text(json.dumps(fixtures, indent=1))
     logs = {
         "ising": {"script": (Path(args.ref) / "examples/ising/in.ising").read_text().splitlines(),

@@ -90,3 +90,32 @@ def test_philox_script_through_driver(sg, ref_fixtures, kind, k):
             line = f"seed {philox_seed}"
         spk.command(line)
     spk.close()
+
+
+def stats_table(text):
+    header, rows = None, []
+    for line in text.splitlines():
+        p = line.split()
+        if p[:4] == ["Time", "Naccept", "Nreject", "Nsweeps"]:
+            header = p
+            continue
+        if header is not None and len(p) == len(header) and p[0][0].isdigit():
+            rows.append(p)
+    return header, rows
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_diag_columns_match_reference_log(sg, ref_fixtures, k):
+    """`diag_style energy | array | cluster` columns printed by the driver from
+    the device diagnostics equal the unmodified reference's (color/strict)."""
+    fx = ref_fixtures["diag_logs"][k]
+    with tempfile.TemporaryDirectory() as d:
+        log = Path(d) / "log.spkgpu"
+        spk = sg.SPPARKS(cmdargs=["-screen", "none", "-log", str(log)])
+        for line in fx["case"]["lines"]:
+            spk.command(line)
+        spk.close()
+        header, rows = stats_table(log.read_text())
+    assert header == fx["header"]
+    drop_cpu = lambda r: r[:4] + r[5:]  # noqa: E731
+    assert [drop_cpu(r) for r in rows] == [drop_cpu(r) for r in fx["rows"]]

@@ -135,3 +135,68 @@ def test_example_log_ising(example_logs):
 
 def test_example_log_potts(example_logs):
     example_run(example_logs, "potts", 2)
+
+
+def parse_diag_script(lines):
+    """Lattice, app and diagnostics of a diag log case script."""
+    spec = {"diags": []}
+    for line in lines:
+        w = line.split()
+        if w[0] == "seed":
+            spec["seed"] = int(w[1])
+        elif w[0] == "app_style":
+            spec["app"] = w[1]
+            spec["q"] = int(w[2]) if len(w) > 2 else 2
+        elif w[0] == "lattice":
+            spec["lattice"] = w[1]
+        elif w[0] == "region":
+            b = [float(v) for v in w[3:9]]
+            spec["n"] = (int(b[1] - b[0]), int(b[3] - b[2]), max(1, int(b[5] - b[4])))
+        elif w[0] == "temperature":
+            spec["T"] = float(w[1])
+        elif w[0] == "diag_style":
+            if w[1] == "array":
+                spec["diags"] += [("array", w[k], w[k + 1]) for k in range(2, len(w), 2)]
+            else:
+                spec["diags"].append((w[1],))
+    return spec
+
+
+def diag_tokens(cfg, spin, diags):
+    """The diag columns the reference prints (%10g / %10d) for a lattice."""
+    out = []
+    for d in diags:
+        if d[0] == "energy":
+            out.append("%g" % oracle.energy(cfg, spin))
+        elif d[0] == "cluster":
+            c = oracle.clusters(cfg, spin)
+            out += ["%d" % c["ncluster"], "%g" % c["mean_volume"], "%g" % c["mean_radius"]]
+        else:
+            v = {"mean": float(np.sum(spin, dtype=np.int64)) / spin.size, "sum": float(np.sum(spin, dtype=np.int64)),
+                 "min": float(spin.min()), "max": float(spin.max())}[d[2]]
+            out.append("%g" % v)
+    return out
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_diagnostics_match_unmodified_reference_log(ref_fixtures, k):
+    """energy, `diag_style array` and `diag_style cluster` columns of an
+    unmodified reference run (sweep color/strict) from the oracle: the t = 0
+    row pins the cluster analysis on the `set site range` lattice, the later
+    rows on the lattices the strict sweeps produce."""
+    fx = ref_fixtures["diag_logs"][k]
+    sp = parse_diag_script(fx["case"]["lines"])
+    nx, ny, nz = sp["n"]
+    cfg = oracle.make_cfg(sp["lattice"], nx, ny, nz, sp["app"], sp["q"], sp["T"], rng=oracle.RNG_STRICT, seed=0)
+    n = nx * ny * nz
+    u = oracle.ranmars_draws(sp["seed"], 5)
+    spin = oracle.set_range(oracle.park_seed(u[0]), n, 1, sp["q"])
+    seeds = oracle.strict_siteseeds(u[4], n)
+    done = naccept = nattempt = 0
+    for row in fx["rows"]:
+        sweeps = int(row[3]) - done
+        if sweeps:
+            na, nt, _ = oracle.color_sweeps(cfg, spin, done, sweeps, siteseeds=seeds)
+            naccept, nattempt, done = naccept + na, nattempt + nt, done + sweeps
+        assert [int(row[1]), int(row[2])] == [naccept, nattempt - naccept]
+        assert diag_tokens(cfg, spin, sp["diags"]) == row[5:], fx["case"]["name"]
