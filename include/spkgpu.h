@@ -149,7 +149,10 @@ int spkgpu_launch_count(const spkgpu_lattice *h, int64_t *count);
 /* rejection-free KMC with the tree solver over sectors --------------------
    adapt = 1: `sector ... nstop N` (dt_kmc = N / max per-site propensity),
    adapt = 0: `sector ... tstop dt`.  fp64 = 1 computes propensities in FP64
-   (bit-exact mode), 0 in FP32; tree sums and the clock are FP64 always.
+   (bit-exact mode); 0 and 2 in FP32, with tree sums, roots and the clock in
+   FP64 always.  fp64 = 0 also keeps an all-FP64 shadow of every pass's
+   per-chain propensity sums (one extra propensity evaluation per site and
+   pass) and reports its errors in the run's stats; fp64 = 2 runs without it.
    spkgpu_kmc_run performs one `run` from *time to stoptime. */
 typedef struct spkgpu_kmc_stats {
   double time;          /* simulated time reached */
@@ -157,6 +160,10 @@ typedef struct spkgpu_kmc_stats {
   int64_t npass;        /* passes over all sectors (cumulative) */
   double dt_kmc;        /* current sector time increment */
   double total_propensity; /* sum of all tree roots after the run */
+  double prop_rel_err;  /* fp64 = 0: relative error of the final lattice's total propensity
+                           from FP32 site propensities against all-FP64 (else 0) */
+  double dt_rel_err;    /* fp64 = 0: max relative error of the run's adaptive time steps
+                           nstop/pmax against all-FP64 propensities (else 0) */
 } spkgpu_kmc_stats;
 int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, double tstop, int32_t fp64);
 int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_stats *out);

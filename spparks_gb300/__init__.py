@@ -68,7 +68,8 @@ class Stats(ctypes.Structure):
 
 class KmcStats(ctypes.Structure):
     _fields_ = [("time", ctypes.c_double), ("naccept", ctypes.c_int64), ("npass", ctypes.c_int64),
-                ("dt_kmc", ctypes.c_double), ("total_propensity", ctypes.c_double)]
+                ("dt_kmc", ctypes.c_double), ("total_propensity", ctypes.c_double),
+                ("prop_rel_err", ctypes.c_double), ("dt_rel_err", ctypes.c_double)]
 
 
 class EnsembleDesc(ctypes.Structure):
@@ -289,16 +290,19 @@ class Lattice:
         self._check(self.lib.spkgpu_launch_count(self.h, ctypes.byref(c)))
         return c.value
 
-    def kmc_setup(self, adapt=True, nstop=1.0, tstop=0.0, fp64=True):
-        self._check(self.lib.spkgpu_kmc_setup(self.h, int(bool(adapt)), float(nstop), float(tstop),
-                                              int(bool(fp64))))
+    def kmc_setup(self, adapt=True, nstop=1.0, tstop=0.0, fp64=True, shadow=True):
+        """fp64: FP64 propensities (bit-exact); else FP32 propensities, with the
+        all-FP64 shadow of the per-chain sums when `shadow`."""
+        mode = 1 if fp64 else (0 if shadow else 2)
+        self._check(self.lib.spkgpu_kmc_setup(self.h, int(bool(adapt)), float(nstop), float(tstop), mode))
 
     def kmc_run(self, time: float, stoptime: float) -> dict:
         t = ctypes.c_double(time)
         s = KmcStats()
         self._check(self.lib.spkgpu_kmc_run(self.h, ctypes.byref(t), float(stoptime), ctypes.byref(s)))
         return {"time": s.time, "naccept": s.naccept, "npass": s.npass, "dt_kmc": s.dt_kmc,
-                "total_propensity": s.total_propensity}
+                "total_propensity": s.total_propensity, "prop_rel_err": s.prop_rel_err,
+                "dt_rel_err": s.dt_rel_err}
 
 
 class Ensemble:

@@ -148,6 +148,34 @@ __global__ void kmc_prop_kernel(KmcArgs a, const int32_t *list, int64_t nlist) {
   }
 }
 
+// per-chain total propensity from the current lattice (the shadow of an
+// FP32 run): site_propensity with FP64 (fp64 = 1) or FP32 Boltzmann factors,
+// summed per chain in FP64 (sites of sector iset only, or all for iset < 0)
+template <typename S, int LAT, int APP>
+__global__ void kmc_sum64_kernel(KmcArgs a, double *chain_sum, int iset, int fp64) {
+  const S *spin = (const S *)a.spin;
+  a.fp64 = fp64;
+  const int64_t n = (int64_t)a.nx * a.ny * a.nz;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = a.setof[i];
+    if (iset >= 0 && c % a.nsector != iset) continue;
+    const double p = site_propensity<S, LAT, APP>(a, spin, i);
+    if (p != 0.0) atomicAdd(&chain_sum[c], p);
+  }
+}
+
+// max over the chains of sector iset (all chains for iset < 0) of
+// sum/num_active, into *bits (non-negative doubles order as their bits)
+__global__ void kmc_pmax64_kernel(KmcArgs a, const double *chain_sum, int iset, int nt, unsigned long long *bits) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    const int c = iset < 0 ? t : t * a.nsector + iset;
+    const int na = a.c_nactive[c];
+    if (na <= 0) continue;
+    const double v = chain_sum[c] / na;
+    atomicMax(bits, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
 // bottom-up rebuild of the trees of chains (proc*nsector + iset), one CTA
 // per chain (iset < 0: every chain), and the count of positive leaves
 __global__ void kmc_build_kernel(KmcArgs a, int iset) {
@@ -342,6 +370,10 @@ struct KmcState {
   double *d_trees = nullptr;
   unsigned long long *d_scalars = nullptr;  // [0] pmax bits, [1] naccept
   std::vector<int32_t> h_nactive;
+  // FP32 runs with the FP64 shadow (fp64 == 0): per-chain FP64 sums
+  int shadow = 0;
+  double *d_sum64 = nullptr;
+  double dt_rel_err = 0.0;    // max relative error of dt_kmc = nstop/pmax against FP64, last run
 };
 
 void spk_kmc_free(spkgpu_lattice *h) {
@@ -360,6 +392,7 @@ void spk_kmc_free(spkgpu_lattice *h) {
   cudaFree(k->d_events);
   cudaFree(k->d_trees);
   cudaFree(k->d_scalars);
+  cudaFree(k->d_sum64);
   delete k;
   h->kmc = nullptr;
 }
@@ -416,6 +449,17 @@ static cudaError_t launch_prop_t(int app, const KmcArgs &a, const int32_t *list,
 }
 
 template <typename S, int LAT>
+static cudaError_t launch_sum64_t(int app, const KmcArgs &a, double *chain_sum, int iset, int fp64, int64_t n,
+                                  cudaStream_t s, int sms) {
+  int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16);
+  if (app == SPKGPU_ISING)
+    kmc_sum64_kernel<S, LAT, SPKGPU_ISING><<<(unsigned)blocks, 256, 0, s>>>(a, chain_sum, iset, fp64);
+  else
+    kmc_sum64_kernel<S, LAT, SPKGPU_POTTS><<<(unsigned)blocks, 256, 0, s>>>(a, chain_sum, iset, fp64);
+  return cudaGetLastError();
+}
+
+template <typename S, int LAT>
 static cudaError_t launch_events_t(int app, const KmcArgs &a, int iset, int nprocs, size_t smem, cudaStream_t s) {
   if (app == SPKGPU_ISING) {
     auto f = kmc_event_kernel<S, LAT, SPKGPU_ISING>;
@@ -444,6 +488,54 @@ static cudaError_t dispatch_lat(int lattice, int app, int what, const KmcArgs &a
   }
 #undef SPK_KMC_CASE
   return cudaErrorInvalidValue;
+}
+
+template <typename S>
+static cudaError_t sum64_lat(int lattice, int app, const KmcArgs &a, double *chain_sum, int iset, int fp64,
+                             int64_t n, cudaStream_t s, int sms) {
+  switch (lattice) {
+    case SPKGPU_SQ_4N: return launch_sum64_t<S, SPKGPU_SQ_4N>(app, a, chain_sum, iset, fp64, n, s, sms);
+    case SPKGPU_SQ_8N: return launch_sum64_t<S, SPKGPU_SQ_8N>(app, a, chain_sum, iset, fp64, n, s, sms);
+    case SPKGPU_SC_6N: return launch_sum64_t<S, SPKGPU_SC_6N>(app, a, chain_sum, iset, fp64, n, s, sms);
+    case SPKGPU_SC_26N: return launch_sum64_t<S, SPKGPU_SC_26N>(app, a, chain_sum, iset, fp64, n, s, sms);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// the all-FP64 shadow of the propensity sums of the chains of sector iset
+// (every chain for iset < 0) at this point of the run: their sums into
+// k->d_sum64 and max(sum/num_active) into k->d_scalars[2] (bits, max-ed)
+static cudaError_t kmc_shadow64(spkgpu_lattice *h, const KmcArgs &a, int iset, int fp64 = 1) {
+  KmcState *k = h->kmc;
+  const int nprocs = k->nchains / h->d.nsector;
+  cudaError_t e = cudaErrorInvalidValue;
+  double *cs = k->d_sum64;
+  switch (h->spin_bytes) {
+    case 1: e = sum64_lat<int8_t>(h->d.lattice, h->d.app, a, cs, iset, fp64, h->n, h->stream, h->num_sms); break;
+    case 2: e = sum64_lat<int16_t>(h->d.lattice, h->d.app, a, cs, iset, fp64, h->n, h->stream, h->num_sms); break;
+    case 4: e = sum64_lat<int32_t>(h->d.lattice, h->d.app, a, cs, iset, fp64, h->n, h->stream, h->num_sms); break;
+  }
+  if (e != cudaSuccess) return e;
+  const int nt = iset < 0 ? k->nchains : nprocs;
+  kmc_pmax64_kernel<<<(nt + 255) / 256, 256, 0, h->stream>>>(a, k->d_sum64, iset, nt, k->d_scalars + 2);
+  h->launches += 2;
+  return cudaGetLastError();
+}
+
+// the shadow's pmax (as max-ed since the last clear) and the sum of the
+// per-chain sums
+static int kmc_shadow_read(spkgpu_lattice *h, double *pmax64, double *total64) {
+  KmcState *k = h->kmc;
+  unsigned long long bits = 0;
+  std::vector<double> sums(k->nchains);
+  KMC_CUDA(h, cudaMemcpyAsync(&bits, k->d_scalars + 2, 8, cudaMemcpyDeviceToHost, h->stream));
+  KMC_CUDA(h, cudaMemcpyAsync(sums.data(), k->d_sum64, k->nchains * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  KMC_CUDA(h, cudaStreamSynchronize(h->stream));
+  memcpy(pmax64, &bits, 8);
+  double tot = 0.0;
+  for (double v : sums) tot += v;
+  *total64 = tot;
+  return SPKGPU_OK;
 }
 
 static cudaError_t kmc_launch(spkgpu_lattice *h, int what, const KmcArgs &a, const int32_t *list, int64_t n,
@@ -476,7 +568,9 @@ extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, 
   k->adapt = adapt ? 1 : 0;
   k->nstop = nstop;
   k->tstop = tstop;
-  k->fp64 = fp64 ? 1 : 0;
+  if (fp64 < 0 || fp64 > 2) return spk_fail(h, SPKGPU_ERR_ARG, "fp64 must be 0, 1 or 2");
+  k->fp64 = (fp64 == 1) ? 1 : 0;
+  k->shadow = (fp64 == 0) ? 1 : 0;
   // chain membership from the handle's processor and sector-half tables
   std::vector<int32_t> blob_proc[3], blob_half[3];
   int dims[3] = {d.nx, d.ny, d.nz};
@@ -558,7 +652,8 @@ extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, 
       !dm((void **)&k->d_tree_off, (k->nchains + 1) * 8) || !dm((void **)&k->d_nloc, k->nchains * 4) ||
       !dm((void **)&k->d_leaf0, k->nchains * 4) || !dm((void **)&k->d_ntotal, k->nchains * 4) ||
       !dm((void **)&k->d_nactive, k->nchains * 4) || !dm((void **)&k->d_events, k->nchains * 8) ||
-      !dm((void **)&k->d_trees, tree_off[k->nchains] * 8) || !dm((void **)&k->d_scalars, 4 * 8)) {
+      !dm((void **)&k->d_trees, tree_off[k->nchains] * 8) || !dm((void **)&k->d_scalars, 4 * 8) ||
+      !dm((void **)&k->d_sum64, k->nchains * 8)) {
     spk_kmc_free(h);
     return spk_fail(h, SPKGPU_ERR_NOMEM, "KMC allocation failed");
   }
@@ -619,11 +714,34 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
     }
     k->dt_kmc = (pmax > 0.0) ? k->nstop / pmax : stoptime - time;
   }
+  // FP32 propensities with the FP64 shadow: pmax of the same chains at the
+  // same moments from all-FP64 propensities, and the relative error of the
+  // adaptive time step nstop/pmax it gives
+  k->dt_rel_err = 0.0;
+  auto shadow_err = [&](double pmax32) -> int {
+    double pmax64 = 0.0, tot64 = 0.0;
+    int rc = kmc_shadow_read(h, &pmax64, &tot64);
+    if (rc) return rc;
+    if (pmax32 > 0.0 && pmax64 > 0.0)
+      k->dt_rel_err = std::max(k->dt_rel_err, fabs(pmax64 / pmax32 - 1.0));  // (1/p32 - 1/p64) / (1/p64)
+    return SPKGPU_OK;
+  };
+  auto shadow_clear = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(k->d_sum64, 0, k->nchains * sizeof(double), h->stream);
+    return e == cudaSuccess ? cudaMemsetAsync(k->d_scalars + 2, 0, 8, h->stream) : e;
+  };
+  if (k->shadow && k->adapt) {
+    KMC_CUDA(h, shadow_clear());
+    KMC_CUDA(h, kmc_shadow64(h, a, -1));
+    int rc = shadow_err(k->nstop / k->dt_kmc);
+    if (rc) return rc;
+  }
   k->dt_kmc = std::min(k->dt_kmc, stoptime - time);
   if (stoptime > time) {
     bool alldone = false;
     while (!alldone) {
       KMC_CUDA(h, cudaMemsetAsync(k->d_scalars, 0, 8, h->stream));
+      if (k->shadow) KMC_CUDA(h, shadow_clear());
       a.dt_kmc = k->dt_kmc;
       for (int iset = 0; iset < nsec; iset++) {
         int64_t b0 = k->border_off[iset], b1 = k->border_off[iset + 1];
@@ -631,6 +749,8 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
         kmc_build_kernel<<<k->nchains / nsec, 256, 0, h->stream>>>(a, iset);
         h->launches++;
         KMC_CUDA(h, cudaGetLastError());
+        // pmax is taken here, before the sector's events (src/app_lattice.cpp:564-571)
+        if (k->shadow) KMC_CUDA(h, kmc_shadow64(h, a, iset));
         KMC_CUDA(h, kmc_launch(h, 1, a, nullptr, 0, iset));
       }
       k->npass++;
@@ -640,6 +760,10 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
         double pmax = 0.0;
         int rc = kmc_pmax(h, &pmax);
         if (rc) return rc;
+        if (k->shadow) {
+          rc = shadow_err(pmax);
+          if (rc) return rc;
+        }
         k->dt_kmc = (pmax > 0.0) ? k->nstop / pmax : stoptime - time;
         k->dt_kmc = std::min(k->dt_kmc, stoptime - time);
       }
@@ -663,6 +787,23 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
     out->npass = k->npass;
     out->dt_kmc = k->dt_kmc;
     out->total_propensity = total;
+    out->prop_rel_err = 0.0;
+    out->dt_rel_err = 0.0;
+    if (k->shadow) {
+      // the final lattice's total propensity from FP32 and from FP64 site
+      // propensities (both summed in FP64)
+      double pm = 0.0, tot32 = 0.0, tot64 = 0.0;
+      KMC_CUDA(h, shadow_clear());
+      KMC_CUDA(h, kmc_shadow64(h, a, -1, 0));
+      int rc = kmc_shadow_read(h, &pm, &tot32);
+      if (rc) return rc;
+      KMC_CUDA(h, shadow_clear());
+      KMC_CUDA(h, kmc_shadow64(h, a, -1, 1));
+      rc = kmc_shadow_read(h, &pm, &tot64);
+      if (rc) return rc;
+      out->prop_rel_err = tot64 > 0.0 ? fabs(tot32 - tot64) / tot64 : 0.0;
+      out->dt_rel_err = k->dt_rel_err;
+    }
   }
   return SPKGPU_OK;
 }

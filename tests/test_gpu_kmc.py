@@ -88,3 +88,27 @@ def test_kmc_fp32_propensity_error(sg):
         st = lat.kmc_run(0.0, 0.0)
         tot[fp64] = st["total_propensity"]
     assert abs(tot[False] - tot[True]) / tot[True] < 1e-6
+
+
+def test_kmc_fp32_run_states_its_error_against_fp64(sg):
+    """An FP32-propensity run (FP64 tree sums, roots and clock) states its
+    precision against all-FP64 propensities: the largest relative error of
+    its adaptive time steps nstop/pmax (pmax sampled where the reference
+    samples it) and of the final lattice's total propensity, both < 1e-6;
+    an FP64 run reports zero for both."""
+    seed = 31
+    nx = ny = 64
+    spin = oracle.init_spins(seed, nx * ny, 1, 20)
+    for fp64 in (False, True):
+        lat = sg.Lattice("sq/8n", nx, ny, 1, "potts", 20, nsector=4, procs=(4, 4, 1), seed=seed)
+        lat.set_temperature(0.8)
+        lat.upload(spin)
+        lat.kmc_setup(fp64=fp64)
+        st = lat.kmc_run(0.0, 2.0)
+        assert st["naccept"] > 1000 and st["npass"] > 2
+        if fp64:
+            assert (st["dt_rel_err"], st["prop_rel_err"]) == (0.0, 0.0)
+        else:
+            assert 0.0 < st["dt_rel_err"] < 1e-6
+            assert 0.0 < st["prop_rel_err"] < 1e-6
+        lat.close()
