@@ -341,6 +341,8 @@ def run_ours(args):
     kernel_ms = kern_ms / max(kern_launches, 1)
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     traffic, traffic_src = profile_traffic(kname)
+    # the draw-side ceiling: one Philox4x32-10 block per x-pair of sites
+    philox_bps = sg.philox_rate(device)
 
     if rank != 0:
         return
@@ -374,6 +376,9 @@ def run_ours(args):
                      "alg_bytes_per_launch": alg_bytes, "kernel_ms_per_launch": kernel_ms,
                      "kernel": kname + (" (one launch per step of 10 sweeps + exchange)" if persistent
                                         else " (one launch per sweep)")},
+        "rng_ceiling": {"philox_blocks_per_s": philox_bps, "site_updates_per_s": 2.0 * philox_bps,
+                        "frac": value / world / (2.0 * philox_bps),
+                        "source": "spkgpu_philox_rate: the sweeps' Philox code alone, 2 sites per block"},
         "cpu_baseline": cpu,
         "clocks": clk,
         "exchange": {"tries": st["exchange_tries"], "accepts": st["exchange_accepts"]},

@@ -168,6 +168,14 @@ typedef struct spkgpu_kmc_stats {
 int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, double tstop, int32_t fp64);
 int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_stats *out);
 
+/* integer-issue ceiling ------------------------------------------------------
+   No counterpart in the reference.  Philox4x32-10 blocks per second that
+   device computes with the sweep kernels' own Philox code and nothing else
+   (iters blocks x 4 per thread, 8 CTAs of 128 threads per SM); a sweep
+   spends one block per x-pair of sites, so 2 x this rate bounds every sweep
+   of the Philox draw contract. */
+int spkgpu_philox_rate(int32_t device, int32_t iters, double *blocks_per_s);
+
 /* sweeping without allocating ----------------------------------------------
    No counterpart in the reference.  For callers that cannot allocate device
    memory themselves or through this library: those that own all of it via

@@ -101,7 +101,7 @@ EXPORTS = [
     "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
     "spkgpu_ensemble_get_stats", "spkgpu_ensemble_temperatures", "spkgpu_ensemble_energies",
     "spkgpu_ensemble_launch_count", "spkgpu_ensemble_mode", "spkgpu_ensemble_sweep_kernel_ms",
-    "spkgpu_sweep_sq4_noalloc",
+    "spkgpu_sweep_sq4_noalloc", "spkgpu_philox_rate",
     "spparks_open_no_mpi", "spparks_close", "spparks_file", "spparks_command", "spparks_extract", "spparks_energy",
     "spkgpu_driver_error", "spkgpu_driver_time",
 ]
@@ -162,9 +162,21 @@ def load_library(path: Path | None = None):
     L.spkgpu_sweep_sq4_noalloc.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_int32, ctypes.c_double, ctypes.c_uint32, ctypes.c_int64,
                                            ctypes.c_int32, vp, P(ctypes.c_int64)]
+    L.spkgpu_philox_rate.argtypes = [ctypes.c_int32, ctypes.c_int32, P(ctypes.c_double)]
     if path is None:
         _lib = L
     return L
+
+
+def philox_rate(device: int = 0, iters: int = 4096) -> float:
+    """Philox4x32-10 blocks/s of the device with the sweeps' own code
+    (spkgpu_philox_rate): half the draw-side ceiling of any sweep."""
+    lib = load_library()
+    v = ctypes.c_double()
+    rc = lib.spkgpu_philox_rate(int(device), int(iters), ctypes.byref(v))
+    if rc != 0:
+        raise SpkGpuError(rc, "spkgpu_philox_rate failed")
+    return v.value
 
 
 def _i32p(a):

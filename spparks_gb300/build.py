@@ -29,6 +29,7 @@ SOURCES = [
     "packed.cu",
     "sweep_rows.cu",
     "diag.cu",
+    "calib.cu",
     "driver.cpp",
 ]
 

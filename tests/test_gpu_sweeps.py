@@ -154,3 +154,8 @@ def test_energy_matches_oracle(sg):
     lat.upload(spin)
     cfg = oracle.make_cfg("sc/26n", 20, 20, 20, "potts", 40)
     assert lat.energy() == oracle.energy(cfg, spin)
+
+
+def test_philox_rate_calibration(sg):
+    """the draw-side ceiling the bench reports: Philox blocks/s of the device"""
+    assert sg.philox_rate(0, 256) > 1e10
