@@ -16,7 +16,7 @@ namespace {
 constexpr int kCalibThreads = 128;
 constexpr int kCalibIlp = 4;
 
-__global__ void __launch_bounds__(kCalibThreads) philox_rate_kernel(uint32_t seed, int iters, uint32_t *out) {
+__global__ void __launch_bounds__(kCalibThreads, 8) philox_rate_kernel(uint32_t seed, int iters, uint32_t *out) {
   const RoundKeys rk = round_keys(seed, kStreamSweep);
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t acc = 0;
@@ -45,14 +45,20 @@ extern "C" int spkgpu_philox_rate(int32_t device, int32_t iters, double *blocks_
   int rc = SPKGPU_OK;
   if (cudaMalloc(&out, (size_t)grid * spk::kCalibThreads * 4) != cudaSuccess) return SPKGPU_ERR_NOMEM;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = SPKGPU_ERR_CUDA;
+  // best of three timed launches after three warm-up launches
   float ms = 0.0f;
   if (rc == SPKGPU_OK) {
     for (int w = 0; w < 3; w++) spk::philox_rate_kernel<<<grid, spk::kCalibThreads>>>(12345u, iters, out);
-    cudaEventRecord(e0);
-    spk::philox_rate_kernel<<<grid, spk::kCalibThreads>>>(12345u, iters, out);
-    cudaEventRecord(e1);
-    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.0f)
-      rc = SPKGPU_ERR_CUDA;
+    for (int r = 0; r < 3 && rc == SPKGPU_OK; r++) {
+      float t = 0.0f;
+      cudaEventRecord(e0);
+      spk::philox_rate_kernel<<<grid, spk::kCalibThreads>>>(12345u, iters, out);
+      cudaEventRecord(e1);
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess || t <= 0.0f)
+        rc = SPKGPU_ERR_CUDA;
+      else if (ms == 0.0f || t < ms)
+        ms = t;
+    }
   }
   if (rc == SPKGPU_OK)
     *blocks_per_s = (double)grid * spk::kCalibThreads * (double)iters * spk::kCalibIlp / (ms * 1e-3);

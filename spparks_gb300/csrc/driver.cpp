@@ -18,9 +18,15 @@
 //                                   DiagCluster (src/diag_*.cpp), computed on
 //                                   the device (spkgpu_energy/site_stats/
 //                                   clusters)
+//   dump ID text|sites DT FILE [id site x y z energy i1]   (src/dump_text.cpp,
+//                                   src/dump_sites.cpp), dump_modify ID
+//                                   delay|delta|flush|tol, undump ID, dump_one ID
+//   read_sites FILE                 Values section (src/read_sites.cpp)
 //   run DT [upto] [pre yes|no] [post yes|no]    (App::run, src/app.cpp:86-148)
-// Output-only commands (dump, the cluster diagnostic's files, ...) are
-// accepted and ignored with a warning.  `sweep random|raster` (serial by definition) is
+// Stats, diagnostics and dumps follow Output::setup/compute
+// (src/output.cpp:82-201).  With solve_style tree, output happens at the
+// start and the end of a run only.  Other output-only commands (the cluster
+// diagnostic's files, ...) are accepted and ignored with a warning.  `sweep random|raster` (serial by definition) is
 // refused.  Errors are printed as "ERROR: ..." like Error::all, but the
 // process is not terminated: the command returns NULL and the message stays
 // readable through spkgpu_driver_error().
@@ -40,12 +46,15 @@
 #include <string.h>
 #include <sys/time.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
 #include "../../include/spkgpu.h"
 
 namespace {
+
+std::vector<std::string> split_words(const char *line);
 
 // Marsaglia RNG of RanMars (src/random_mars.cpp:43-105): the published
 // universal generator of Marsaglia, Zaman and Tsang
@@ -162,6 +171,18 @@ struct Driver {
     std::vector<int> methods;  // array: one column per (i1, method) pair
   };
   std::vector<DiagSpec> diags;
+  // dumps in declaration order
+  enum { F_ID, F_SITE, F_X, F_Y, F_Z, F_ENERGY };
+  struct DumpSpec {
+    std::string id, style, filename, columns, columns_orig;
+    double delta = 0.0, delay = 0.0, tolerance = 0.0, next_time = 0.0;
+    std::vector<int> fields;
+    bool multifile = false, flush = true, first = true;
+    int idump = 0, pad = 0;
+    FILE *fp = nullptr;  // the single file, open from the first run on
+  };
+  std::vector<DumpSpec> dumps;
+  double stats_time = 0.0;
   // run state
   double time = 0.0;
   int64_t nsweeps = 0, naccept = 0, nattempt = 0;
@@ -178,6 +199,8 @@ struct Driver {
 
   ~Driver() {
     if (h) spkgpu_destroy(h);
+    for (DumpSpec &d : dumps)
+      if (d.fp) fclose(d.fp);
     if (logfile) fclose(logfile);
   }
 
@@ -227,6 +250,15 @@ struct Driver {
   bool ensure_handle();
   bool sync_to_host();
   void stats_line(double cpu);
+  // output (src/output.cpp)
+  static double next_time(double t, double delta, double delay);
+  bool output_setup(double stoptime, double *tnext);
+  bool output_compute(double stoptime, bool done, double cpu, double *tnext);
+  bool dump_command(std::vector<std::string> &w);
+  bool dump_modify(std::vector<std::string> &w);
+  bool dump_write(DumpSpec &d);
+  bool read_sites(const std::string &file);
+  bool current_sites(std::vector<int32_t> &out);
 };
 
 double wall() {
@@ -427,6 +459,310 @@ std::string Driver::diag_values() {
   return out;
 }
 
+// Output::next_time without log spacing (src/output.cpp:414-437)
+double Driver::next_time(double t, double delta, double delay) {
+  double tnew = ceil(t / delta) * delta;
+  if (tnew == t) tnew = t + delta;
+  return tnew > delay ? tnew : delay;
+}
+
+// the site values as they are now: the host copy, or the device's during a run
+bool Driver::current_sites(std::vector<int32_t> &out) {
+  if (host_valid || !h || !device_valid) {
+    out = site;
+    return true;
+  }
+  out.resize(n());
+  if (spkgpu_download_spins(h, out.data(), n()) != 0) return fail(spkgpu_last_error(h));
+  return true;
+}
+
+// neighbour offsets of the lattice style (CreateSites::offsets_2d/3d,
+// src/create_sites.cpp:1303-1371)
+static void lattice_offsets(int lattice, std::vector<int> &dx, std::vector<int> &dy, std::vector<int> &dz) {
+  const bool is3d = lattice >= 2;
+  for (int a = -1; a <= 1; a++)
+    for (int b = -1; b <= 1; b++)
+      for (int c = is3d ? -1 : 0; c <= (is3d ? 1 : 0); c++) {
+        const int r2 = a * a + b * b + c * c;
+        const bool keep = (lattice == 0 || lattice == 2) ? r2 == 1 : r2 >= 1;
+        if (!keep) continue;
+        dx.push_back(a);
+        dy.push_back(b);
+        dz.push_back(c);
+      }
+}
+
+// Dump::write with the DumpText (src/dump_text.cpp:347-421) and DumpSites
+// (src/dump_sites.cpp:51-67) headers; one process, so rows in id order
+bool Driver::dump_write(DumpSpec &d) {
+  std::vector<int32_t> v;
+  if (!current_sites(v)) return false;
+  FILE *fp = d.fp;
+  if (d.multifile) {
+    const size_t star = d.filename.find('*');
+    char num[32];
+    snprintf(num, sizeof(num), "%0*d", d.pad, d.idump);
+    const std::string name = d.filename.substr(0, star) + num + d.filename.substr(star + 1);
+    fp = fopen(name.c_str(), "w");
+    if (!fp) return fail("Cannot open dump file " + name);
+  } else if (!fp) {
+    d.fp = fp = fopen(d.filename.c_str(), "w");
+    if (!fp) return fail("Cannot open dump file " + d.filename);
+  }
+  const long long nd = (long long)n();
+  const double zlo = dimension == 2 ? -0.5 : 0.0, zhi = dimension == 2 ? 0.5 : (double)nz;
+  if (d.style == "sites") {
+    fprintf(fp, "Site file written by dump sites %s command at time: %d %g\n\n", d.id.c_str(), d.idump, time);
+    fprintf(fp, "%d dimension\n", dimension);
+    fprintf(fp, "%lld sites\n", nd);
+    fprintf(fp, "%s values\n", d.columns_orig.c_str());
+    fprintf(fp, "%g %g xlo xhi\n", 0.0, (double)nx);
+    fprintf(fp, "%g %g ylo yhi\n", 0.0, (double)ny);
+    fprintf(fp, "%g %g zlo zhi\n", zlo, zhi);
+    fprintf(fp, "\nValues\n\n");
+  } else {
+    fprintf(fp, "ITEM: TIMESTEP\n");
+    fprintf(fp, "%d %10g\n", d.idump, time);
+    fprintf(fp, "ITEM: NUMBER OF ATOMS\n");
+    fprintf(fp, "%lld\n", nd);
+    fprintf(fp, "ITEM: BOX BOUNDS\n");
+    fprintf(fp, "%g %g\n", 0.0, (double)nx);
+    fprintf(fp, "%g %g\n", 0.0, (double)ny);
+    fprintf(fp, "%g %g\n", zlo, zhi);
+    fprintf(fp, "ITEM: ATOMS %s\n", d.columns.c_str());
+  }
+  std::vector<int> ox, oy, oz;
+  lattice_offsets(lattice, ox, oy, oz);
+  for (int64_t i = 0; i < (int64_t)nd; i++) {
+    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
+    for (int f : d.fields) {
+      switch (f) {
+        case F_ID: fprintf(fp, "%d ", (int)(i + 1)); break;
+        case F_SITE: fprintf(fp, "%d ", v[i]); break;
+        case F_X: fprintf(fp, "%g ", (double)x); break;
+        case F_Y: fprintf(fp, "%g ", (double)y); break;
+        case F_Z: fprintf(fp, "%g ", (double)z); break;
+        default: {
+          // site_energy: unlike neighbours (src/app_potts.cpp:97-104)
+          int e = 0;
+          for (size_t j = 0; j < ox.size(); j++) {
+            const int xn = (x + ox[j] + nx) % nx, yn = (y + oy[j] + ny) % ny, zn = (z + oz[j] + nz) % nz;
+            e += v[xn + (int64_t)nx * (yn + (int64_t)ny * zn)] != v[i];
+          }
+          fprintf(fp, "%g ", (double)e);
+        }
+      }
+    }
+    fputc('\n', fp);
+  }
+  if (d.flush) fflush(fp);
+  if (d.multifile) fclose(fp);
+  d.first = false;
+  d.idump++;
+  return true;
+}
+
+// Output::setup (src/output.cpp:82-141): first dumps, stats header and row
+bool Driver::output_setup(double stoptime, double *tnext) {
+  double dump_time = stoptime;
+  for (DumpSpec &d : dumps) {
+    if (d.first && time >= d.delay)
+      if (!dump_write(d)) return false;
+    d.next_time = next_time(time + d.tolerance, d.delta, d.delay) - d.tolerance;
+    dump_time = std::min(dump_time, d.next_time);
+  }
+  print("%10s %10s %10s %10s %10s%s\n", "Time", "Naccept", "Nreject", "Nsweeps", "CPU", diag_header().c_str());
+  stats_line(0.0);
+  stats_time = stats_delta > 0.0 ? next_time(time, stats_delta, 0.0) : stoptime;
+  *tnext = std::min(stoptime, std::min(dump_time, stats_time));
+  return true;
+}
+
+// Output::compute (src/output.cpp:148-201): stats row when due or done, then
+// the dumps that are due
+bool Driver::output_compute(double stoptime, bool done, double cpu, double *tnext) {
+  if (time >= stats_time || done) {
+    stats_line(cpu);
+    stats_time = stats_delta > 0.0 ? next_time(time, stats_delta, 0.0) : stoptime;
+  }
+  double dump_time = stoptime;
+  for (DumpSpec &d : dumps) {
+    if (time >= d.next_time - d.tolerance) {
+      if (!dump_write(d)) return false;
+      d.next_time = next_time(time + d.tolerance, d.delta, d.delay) - d.tolerance;
+    }
+    dump_time = std::min(dump_time, d.next_time);
+  }
+  *tnext = std::min(stoptime, std::min(dump_time, stats_time));
+  return true;
+}
+
+// dump ID style DELTA FILE fields (Dump::Dump, src/dump.cpp:40-140;
+// DumpText::parse_fields, src/dump_text.cpp:426-490; DumpSites checks,
+// src/dump_sites.cpp:29-48)
+bool Driver::dump_command(std::vector<std::string> &w) {
+  if (app_id < 0) return fail("Dump command before app_style set");
+  if (w.size() < 5) return fail("Illegal dump command");
+  for (const DumpSpec &o : dumps)
+    if (o.id == w[1]) return fail("Reuse of dump ID");
+  DumpSpec d;
+  d.id = w[1];
+  d.style = w[2];
+  if (d.style != "text" && d.style != "sites") {
+    print("WARNING: dump style %s is not written by the GPU driver\n", d.style.c_str());
+    return true;
+  }
+  if (!parse_double(w[3], &d.delta) || d.delta <= 0.0) return fail("Illegal dump command");
+  d.filename = w[4];
+  auto ends = [&](const char *suf) {
+    size_t k = strlen(suf);
+    return d.filename.size() > k && d.filename.compare(d.filename.size() - k, k, suf) == 0;
+  };
+  if (ends(".bin") || ends(".gz")) return fail("the GPU driver writes text dumps only");
+  size_t pct = d.filename.find('%');
+  if (pct != std::string::npos) {
+    if (d.style == "sites") return fail("Dump sites cannot write multiple files per snapshot");
+    d.filename.replace(pct, 1, "0");  // one process
+  }
+  d.multifile = d.filename.find('*') != std::string::npos;
+  std::vector<std::string> f(w.begin() + 5, w.end());
+  if (f.empty() && d.style == "text") f = {"id", "site", "x", "y", "z"};
+  for (const std::string &a : f) {
+    if (a == "id") d.fields.push_back(F_ID);
+    else if (a == "site" || a == "i1") d.fields.push_back(F_SITE);
+    else if (a == "x") d.fields.push_back(F_X);
+    else if (a == "y") d.fields.push_back(F_Y);
+    else if (a == "z") d.fields.push_back(F_Z);
+    else if (a == "energy") d.fields.push_back(F_ENERGY);
+    else if (a == "propensity") return fail("dump propensity is not written by the GPU driver");
+    else return fail("Invalid keyword in dump command");
+    if (!d.columns.empty()) d.columns += " ";
+    d.columns += a.find("site") != std::string::npos ? "type" : a;
+    if (!d.columns_orig.empty()) d.columns_orig += " ";
+    d.columns_orig += a;
+  }
+  if (d.style == "sites") {
+    if (!d.multifile) return fail("Dump sites must write one file per snapshot");
+    if (d.fields.empty() || d.fields[0] != F_ID) return fail("Dump sites requires ID as first field");
+    if (d.fields.size() < 2) return fail("Dump sites requires two or more fields");
+  }
+  dumps.push_back(d);
+  return true;
+}
+
+// dump_modify ID keyword value ... (Dump::modify_params, src/dump.cpp:640-800)
+bool Driver::dump_modify(std::vector<std::string> &w) {
+  if (w.size() < 2) return fail("Illegal dump_modify command");
+  DumpSpec *d = nullptr;
+  for (DumpSpec &o : dumps)
+    if (o.id == w[1]) d = &o;
+  if (!d) return fail("Could not find dump ID in dump_modify command");
+  for (size_t k = 2; k < w.size(); k += 2) {
+    if (k + 1 >= w.size()) return fail("Illegal dump_modify command");
+    const std::string &key = w[k], &val = w[k + 1];
+    double v = 0.0;
+    if (key == "delay" && parse_double(val, &v)) d->delay = v;
+    else if (key == "delta" && parse_double(val, &v) && v > 0.0) d->delta = v;
+    else if (key == "tol" && parse_double(val, &v) && v >= 0.0) d->tolerance = v;
+    else if (key == "flush" && (val == "yes" || val == "no")) d->flush = val == "yes";
+    else if (key == "pad" && parse_int(val, &d->pad) && d->pad >= 0) {}
+    else return fail("dump_modify " + key + " is not supported by the GPU driver");
+  }
+  return true;
+}
+
+// read_sites FILE: the Values section onto existing sites (ReadSites::command,
+// header, values: src/read_sites.cpp:69-640); Sites/Neighbors sections
+// describe explicit lattices, which the GPU path creates with create_sites
+bool Driver::read_sites(const std::string &file) {
+  if (app_id < 0) return fail("Read_sites command before app_style set");
+  FILE *fp = fopen(file.c_str(), "r");
+  if (!fp) return fail("Cannot open file " + file);
+  print("Reading site file ...\n");
+  char line[4096];
+  std::string columns;
+  bool have_columns = false;
+  auto done_with = [&](bool ok) {
+    fclose(fp);
+    return ok;
+  };
+  if (!fgets(line, sizeof(line), fp)) return done_with(fail("Unexpected end of data file"));
+  std::string keyword;
+  while (fgets(line, sizeof(line), fp)) {
+    if (char *c = strchr(line, '#')) *c = '\0';
+    if (strspn(line, " \t\n\r") == strlen(line)) continue;
+    std::string l = line;
+    double a = 0.0, b = 0.0;
+    if (l.find("dimension") != std::string::npos) {
+      int dim = atoi(line);
+      if (box && dim != dimension) return done_with(fail("Data file dimension does not match existing box"));
+    } else if (l.find("max neighbors") != std::string::npos) {
+      return done_with(fail("read_sites Sites/Neighbors describe explicit lattices; the GPU path uses create_sites"));
+    } else if (l.find("sites") != std::string::npos) {
+      long long ng = atoll(line);
+      if (sites && ng != (long long)n())
+        return done_with(fail("Data file number of sites does not match existing sites"));
+    } else if (l.find("values") != std::string::npos) {
+      columns = l.substr(0, l.find("values"));
+      have_columns = true;
+    } else if (l.find("xlo xhi") != std::string::npos || l.find("ylo yhi") != std::string::npos ||
+               l.find("zlo zhi") != std::string::npos) {
+      sscanf(line, "%lg %lg", &a, &b);
+    } else {
+      size_t s0 = l.find_first_not_of(" \t\n\r"), s1 = l.find_last_not_of(" \t\n\r");
+      keyword = l.substr(s0, s1 - s0 + 1);
+      break;
+    }
+  }
+  bool any = false;
+  while (!keyword.empty()) {
+    if (keyword != "Values")
+      return done_with(fail(keyword == "Sites" || keyword == "Neighbors"
+                                ? "read_sites " + keyword + " sections are not on the GPU path (use create_sites)"
+                                : "Unknown identifier in data file: " + keyword));
+    if (!sites) return done_with(fail("Cannot read Values before sites exist or are read"));
+    if (!fgets(line, sizeof(line), fp)) return done_with(fail("Unexpected end of data file"));  // blank line
+    // columns: "id" then site|i1 (the apps here have one integer per site)
+    std::vector<int> cols;
+    if (!have_columns) {
+      cols.push_back(1);
+    } else {
+      std::vector<std::string> words = split_words(columns.c_str());
+      if (words.size() < 2) return done_with(fail("Read sites Values section has no values per site"));
+      if (words[0] != "id") return done_with(fail("Read sites values header keyword must start with id"));
+      for (size_t k = 1; k < words.size(); k++) {
+        if (words[k] == "site" || words[k] == "i1") cols.push_back(1);
+        else return done_with(fail("Invalid keyword in read sites values header"));
+      }
+    }
+    if (!sync_to_host()) return done_with(false);
+    for (int64_t r = 0; r < n(); r++) {
+      if (!fgets(line, sizeof(line), fp)) return done_with(fail("Unexpected end of data file"));
+      std::vector<std::string> words = split_words(line);
+      if (words.size() != cols.size() + 1) return done_with(fail("Incorrect value format in data file"));
+      long long id = atoll(words[0].c_str());
+      if (id < 1 || id > (long long)n()) continue;  // not a site of this lattice
+      for (size_t k = 0; k < cols.size(); k++) site[id - 1] = atoi(words[k + 1].c_str());
+    }
+    host_valid = true;
+    device_valid = false;
+    any = true;
+    print("  %lld values\n", (long long)n() * (long long)cols.size());
+    // next keyword: skip blank lines, then read the keyword line
+    keyword.clear();
+    while (fgets(line, sizeof(line), fp)) {
+      if (strspn(line, " \t\n\r") == strlen(line)) continue;
+      std::string l = line;
+      size_t s0 = l.find_first_not_of(" \t\n\r"), s1 = l.find_last_not_of(" \t\n\r");
+      keyword = l.substr(s0, s1 - s0 + 1);
+      break;
+    }
+  }
+  if (!any) return done_with(fail("Site file has no Sites, Neighbors, or Values"));
+  return done_with(true);
+}
+
 bool Driver::run(std::vector<std::string> &w) {
   if (app_id < 0) return fail("Run command before app_style set");
   if (!box) return fail("Cannot run application until simulation box is defined");
@@ -476,10 +812,9 @@ bool Driver::run(std::vector<std::string> &w) {
   host_valid = false;
   first_run = false;
   print("Setting up run ...\n");
-  print("%10s %10s %10s %10s %10s%s\n", "Time", "Naccept", "Nreject", "Nsweeps", "CPU", diag_header().c_str());
   double t0 = wall();
-  stats_line(0.0);
-  double nextoutput = stats_delta > 0.0 ? time + stats_delta : stoptime;
+  double nextoutput = stoptime;
+  if (!output_setup(stoptime, &nextoutput)) return false;
   if (tree) {
     spkgpu_kmc_stats ks;
     // one solver state per handle: consecutive runs continue its event
@@ -493,7 +828,7 @@ bool Driver::run(std::vector<std::string> &w) {
       naccept = ks.naccept;
       nsweeps = ks.npass;
     }
-    stats_line(wall() - t0);
+    if (!output_compute(stoptime, true, wall() - t0, &nextoutput)) return false;
   } else {
     // rejection KMC: dt_rkmc = nloop * dt_sweep per pass over all sets
     // (src/app_lattice.cpp:398-420)
@@ -511,9 +846,7 @@ bool Driver::run(std::vector<std::string> &w) {
         if (spkgpu_get_stats(h, &st) != 0) return fail(spkgpu_last_error(h));
         naccept = st.naccept;
         nattempt = st.nattempt;
-        stats_line(wall() - t0);
-        if (stats_delta > 0.0)
-          while (nextoutput <= time) nextoutput += stats_delta;
+        if (!output_compute(stoptime, done, wall() - t0, &nextoutput)) return false;
       }
     }
   }
@@ -672,8 +1005,24 @@ bool Driver::command(std::vector<std::string> &w) {
     return diag_style(w);
   } else if (c == "run") {
     return run(w);
-  } else if (c == "dump" || c == "undump" || c == "dump_modify" || c == "echo" || c == "log" ||
-             c == "diag_style" || c == "reset_time" || c == "shell") {
+  } else if (c == "dump") {
+    return dump_command(w);
+  } else if (c == "dump_modify") {
+    return dump_modify(w);
+  } else if (c == "undump" || c == "dump_one") {
+    if (w.size() != 2) return fail("Illegal " + c + " command");
+    for (size_t k = 0; k < dumps.size(); k++) {
+      if (dumps[k].id != w[1]) continue;
+      if (c == "dump_one") return dump_write(dumps[k]);
+      if (dumps[k].fp) fclose(dumps[k].fp);
+      dumps.erase(dumps.begin() + k);
+      return true;
+    }
+    return fail("Could not find dump ID in " + c + " command");
+  } else if (c == "read_sites") {
+    if (w.size() != 2) return fail("Illegal read_sites command");
+    return read_sites(w[1]);
+  } else if (c == "echo" || c == "log" || c == "reset_time" || c == "shell") {
     print("WARNING: %s is ignored by the GPU driver\n", c.c_str());
   } else {
     return fail("Unknown command: " + c);

@@ -201,6 +201,56 @@ DIAG_LOG_CASES = [
 ]
 
 
+# unmodified reference runs that write dumps (text and sites) or read a site
+# file: the driver must write the same files and print the same stats
+def _site_file():
+    """a Values-only site file for a 12x12 lattice (values 1..5 by a fixed rule)"""
+    rows = [f"{i + 1} {1 + (7 * i + (i // 12) * 3) % 5}" for i in range(144)]
+    return "\n".join(["read_sites input", "", "2 dimension", "144 sites", "id site values",
+                      "0 12 xlo xhi", "0 12 ylo yhi", "-0.5 0.5 zlo zhi", "", "Values", ""] + rows) + "\n"
+
+
+IO_CASES = [
+    dict(name="io_dump_strict_ising_sq4n_16", inputs={}, outputs=["dump.text", "sites.0.txt", "sites.1.txt",
+                                                                  "sites.2.txt"], lines=[
+        "seed 4321", "app_style ising", "dimension 2", "lattice sq/4n 1.0", "region box block 0 16 0 16 -0.5 0.5",
+        "create_box box", "create_sites box", "set site range 1 2", "sweep color/strict", "temperature 2.0",
+        "diag_style energy", "dump 1 text 2.0 dump.text id site x y z energy", "dump 2 sites 5.0 sites.*.txt id site",
+        "stats 2.0", "run 10.0"]),
+    dict(name="io_dump_strict_potts_sc26n_6", inputs={}, outputs=["d3.txt"], lines=[
+        "seed 8642", "app_style potts 6", "dimension 3", "lattice sc/26n 1.0", "region box block 0 6 0 6 0 6",
+        "create_box box", "create_sites box", "set site range 1 6", "sweep color/strict", "temperature 0.7",
+        "dump 1 text 0.5 d3.txt id site energy", "dump_modify 1 delay 1.0", "stats 0.5", "run 2.0", "run 1.0"]),
+    dict(name="io_read_sites_strict_potts_sq8n_12", inputs={"in.sites": _site_file()}, outputs=["final.0.txt"],
+         lines=[
+        "seed 97", "app_style potts 5", "dimension 2", "lattice sq/8n 1.0", "region box block 0 12 0 12 -0.5 0.5",
+        "create_box box", "create_sites box", "read_sites in.sites", "sweep color/strict", "temperature 0.5",
+        "diag_style energy", "stats 1.0", "dump 1 sites 3.0 final.*.txt id site", "dump_modify 1 delay 3.0",
+        "run 3.0"]),
+]
+
+
+def spk_serial_io(binary, case):
+    """Stats table and the written files of a reference run."""
+    with tempfile.TemporaryDirectory(dir=str(ROOT / "oracle" / "_ref")) as d:
+        for name, text in case["inputs"].items():
+            (Path(d) / name).write_text(text)
+        (Path(d) / "in.case").write_text("\n".join(case["lines"]) + "\n")
+        subprocess.run([str(binary), "-in", "in.case", "-screen", "none", "-log", "log.case"], cwd=d, check=True,
+                       capture_output=True)
+        log = (Path(d) / "log.case").read_text()
+        files = {name: (Path(d) / name).read_text() for name in case["outputs"]}
+    header, rows = None, []
+    for line in log.splitlines():
+        p = line.split()
+        if p[:4] == ["Time", "Naccept", "Nreject", "Nsweeps"]:
+            header = p
+            continue
+        if header is not None and len(p) == len(header) and p[0][0].isdigit():
+            rows.append(p[:4] + ["-"] + p[5:])  # CPU seconds vary from run to run
+    return header, rows, files
+
+
 def spk_serial_table(binary, lines):
     """Header tokens and the stats rows (as printed tokens) of a reference run."""
     with tempfile.TemporaryDirectory(dir=str(ROOT / "oracle" / "_ref")) as d:
@@ -217,7 +267,7 @@ def spk_serial_table(binary, lines):
             continue
         if header is not None:
             if len(p) == len(header) and p[0][0].isdigit():
-                rows.append(p)
+                rows.append(p[:4] + ["-"] + p[5:])  # CPU seconds vary from run to run
                 continue
             if rows:
                 break
@@ -302,6 +352,11 @@ def main():
         header, rows = spk_serial_table(serial, case["lines"])
         fixtures["diag_logs"].append({"case": case, "header": header, "rows": rows})
         print("diag log case", case["name"], header, len(rows), "rows")
+    fixtures["io"] = []
+    for case in IO_CASES:
+        header, rows, files = spk_serial_io(serial, case)
+        fixtures["io"].append({"case": case, "header": header, "rows": rows, "files": files})
+        print("io case", case["name"], len(rows), "rows", sorted(files))
     (HERE / "reference_philox.json").write_text(json.dumps(fixtures, indent=1))
     logs = {
         "ising": {"script": (Path(args.ref) / "examples/ising/in.ising").read_text().splitlines(),

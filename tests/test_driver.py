@@ -68,3 +68,32 @@ def test_set_site_range_equals_oracle_restatement(spk):
     spk.command("set site range 1 7")
     u = oracle.ranmars_draws(56789, 1)
     assert spk.sites().tolist() == oracle.set_range(oracle.park_seed(u[0]), 256, 1, 7).tolist()
+
+
+def test_dump_one_and_read_sites_match_reference_files(spk, ref_fixtures, tmp_path, monkeypatch):
+    """Before any run (no device work): `dump_one` writes the reference's
+    first text snapshot of the `set site range` lattice byte for byte, and a
+    `dump sites` file read back with `read_sites` restores the same values."""
+    monkeypatch.chdir(tmp_path)
+    fx = ref_fixtures["io"][0]
+    lines = [ln for ln in fx["case"]["lines"] if not ln.startswith(("run", "stats"))]
+    for line in lines:
+        spk.command(line)
+    spk.command("dump_one 1")
+    first = fx["files"]["dump.text"].split("ITEM: TIMESTEP")[1]
+    assert (tmp_path / "dump.text").read_text() == "ITEM: TIMESTEP" + first
+    spk.command("dump_one 2")
+    assert (tmp_path / "sites.0.txt").read_text() == fx["files"]["sites.0.txt"]
+    before = spk.sites().copy()
+    spk.command("set site value 1")
+    spk.command("read_sites sites.0.txt")
+    assert spk.sites().tolist() == before.tolist()
+
+
+def test_read_sites_refuses_explicit_lattices(spk, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    for line in setup_lines(8, 8, "ising"):
+        spk.command(line)
+    (tmp_path / "s.txt").write_text("x\n\n2 dimension\n64 sites\n4 max neighbors\n\nSites\n\n")
+    with pytest.raises(sg.SpkGpuError, match="create_sites"):
+        spk.command("read_sites s.txt")

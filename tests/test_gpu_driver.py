@@ -119,3 +119,25 @@ def test_diag_columns_match_reference_log(sg, ref_fixtures, k):
     assert header == fx["header"]
     drop_cpu = lambda r: r[:4] + r[5:]  # noqa: E731
     assert [drop_cpu(r) for r in rows] == [drop_cpu(r) for r in fx["rows"]]
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_dumps_and_read_sites_match_reference(sg, ref_fixtures, k, tmp_path, monkeypatch):
+    """`dump text|sites` (with `dump_modify delay`) and `read_sites` through
+    the driver: the stats rows and every file the unmodified reference writes
+    (color/strict runs) are reproduced exactly."""
+    fx = ref_fixtures["io"][k]
+    monkeypatch.chdir(tmp_path)
+    for name, text in fx["case"]["inputs"].items():
+        (tmp_path / name).write_text(text)
+    log = tmp_path / "log.spkgpu"
+    spk = sg.SPPARKS(cmdargs=["-screen", "none", "-log", str(log)])
+    for line in fx["case"]["lines"]:
+        spk.command(line)
+    spk.close()
+    header, rows = stats_table(log.read_text())
+    assert header == fx["header"]
+    drop_cpu = lambda r: r[:4] + r[5:]  # noqa: E731
+    assert [drop_cpu(r) for r in rows] == [drop_cpu(r) for r in fx["rows"]]
+    for name, text in fx["files"].items():
+        assert (tmp_path / name).read_text() == text, name
