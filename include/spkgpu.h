@@ -167,6 +167,14 @@ typedef struct spkgpu_kmc_stats {
 } spkgpu_kmc_stats;
 int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, double tstop, int32_t fp64);
 int spkgpu_kmc_run(spkgpu_lattice *h, double *time, double stoptime, spkgpu_kmc_stats *out);
+/* the same run in pieces, for output during it: first = 1 starts a run (the
+   setup spkgpu_kmc_run does), first = 0 continues the current one; passes
+   stop once *time reaches stoptime (which alone bounds the time steps, as
+   the run's end does in the reference) or, earlier, once a pass ends at or
+   after `until` (the next output time).  Runs equal spkgpu_kmc_run's for
+   any sequence of `until` values. */
+int spkgpu_kmc_run_until(spkgpu_lattice *h, double *time, double stoptime, double until, int32_t first,
+                         spkgpu_kmc_stats *out);
 
 /* integer-issue ceiling ------------------------------------------------------
    No counterpart in the reference.  Philox4x32-10 blocks per second that

@@ -96,7 +96,7 @@ EXPORTS = [
     "spkgpu_upload_spins", "spkgpu_download_spins", "spkgpu_init_spins", "spkgpu_upload_siteseeds", "spkgpu_download_siteseeds",
     "spkgpu_upload_mask", "spkgpu_download_mask", "spkgpu_sweep", "spkgpu_set_sweep_index",
     "spkgpu_get_stats", "spkgpu_energy", "spkgpu_site_stats", "spkgpu_clusters", "spkgpu_synchronize", "spkgpu_timed_sweeps", "spkgpu_stream",
-    "spkgpu_device_spins", "spkgpu_launch_count", "spkgpu_kmc_setup", "spkgpu_kmc_run",
+    "spkgpu_device_spins", "spkgpu_launch_count", "spkgpu_kmc_setup", "spkgpu_kmc_run", "spkgpu_kmc_run_until",
     "spkgpu_ensemble_create", "spkgpu_ensemble_destroy", "spkgpu_ensemble_last_error", "spkgpu_ensemble_upload",
     "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
     "spkgpu_ensemble_get_stats", "spkgpu_ensemble_temperatures", "spkgpu_ensemble_energies",
@@ -144,6 +144,8 @@ def load_library(path: Path | None = None):
     L.spkgpu_launch_count.argtypes = [vp, P(ctypes.c_int64)]
     L.spkgpu_kmc_setup.argtypes = [vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32]
     L.spkgpu_kmc_run.argtypes = [vp, P(ctypes.c_double), ctypes.c_double, P(KmcStats)]
+    L.spkgpu_kmc_run_until.argtypes = [vp, P(ctypes.c_double), ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                       P(KmcStats)]
     L.spkgpu_ensemble_create.argtypes = [P(EnsembleDesc), P(vp)]
     L.spkgpu_ensemble_destroy.argtypes = [vp]
     L.spkgpu_ensemble_last_error.argtypes = [vp]
@@ -308,10 +310,16 @@ class Lattice:
         mode = 1 if fp64 else (0 if shadow else 2)
         self._check(self.lib.spkgpu_kmc_setup(self.h, int(bool(adapt)), float(nstop), float(tstop), mode))
 
-    def kmc_run(self, time: float, stoptime: float) -> dict:
+    def kmc_run(self, time: float, stoptime: float, until: float | None = None, first: bool = True) -> dict:
+        """one KMC run from `time` to `stoptime`; with `until`, only the passes
+        up to that output time (continue with first=False)."""
         t = ctypes.c_double(time)
         s = KmcStats()
-        self._check(self.lib.spkgpu_kmc_run(self.h, ctypes.byref(t), float(stoptime), ctypes.byref(s)))
+        if until is None:
+            self._check(self.lib.spkgpu_kmc_run(self.h, ctypes.byref(t), float(stoptime), ctypes.byref(s)))
+        else:
+            self._check(self.lib.spkgpu_kmc_run_until(self.h, ctypes.byref(t), float(stoptime), float(until),
+                                                      int(bool(first)), ctypes.byref(s)))
         return {"time": s.time, "naccept": s.naccept, "npass": s.npass, "dt_kmc": s.dt_kmc,
                 "total_propensity": s.total_propensity, "prop_rel_err": s.prop_rel_err,
                 "dt_rel_err": s.dt_rel_err}

@@ -22,11 +22,12 @@
 //                                   src/dump_sites.cpp), dump_modify ID
 //                                   delay|delta|flush|tol, undump ID, dump_one ID
 //   read_sites FILE                 Values section (src/read_sites.cpp)
+//   log FILE | none                 Input::log
 //   run DT [upto] [pre yes|no] [post yes|no]    (App::run, src/app.cpp:86-148)
 // Stats, diagnostics and dumps follow Output::setup/compute
-// (src/output.cpp:82-201).  With solve_style tree, output happens at the
-// start and the end of a run only.  Other output-only commands (the cluster
-// diagnostic's files, ...) are accepted and ignored with a warning.  `sweep random|raster` (serial by definition) is
+// (src/output.cpp:82-201), also between the passes of tree KMC.  Other
+// output-only commands (the cluster diagnostic's files, ...) are accepted
+// and ignored with a warning.  `sweep random|raster` (serial by definition) is
 // refused.  Errors are printed as "ERROR: ..." like Error::all, but the
 // process is not terminated: the command returns NULL and the message stays
 // readable through spkgpu_driver_error().
@@ -824,11 +825,20 @@ bool Driver::run(std::vector<std::string> &w) {
       kmc_ready = true;
     }
     if (stoptime > time) {
-      if (spkgpu_kmc_run(h, &time, stoptime, &ks) != 0) return fail(spkgpu_last_error(h));
-      naccept = ks.naccept;
-      nsweeps = ks.npass;
+      // passes up to each output time (src/app_lattice.cpp:517-626)
+      bool done = false, first = true;
+      while (!done) {
+        if (spkgpu_kmc_run_until(h, &time, stoptime, nextoutput, first ? 1 : 0, &ks) != 0)
+          return fail(spkgpu_last_error(h));
+        first = false;
+        naccept = ks.naccept;
+        nsweeps = ks.npass;
+        done = time >= stoptime;
+        if (!output_compute(stoptime, done, wall() - t0, &nextoutput)) return false;
+      }
+    } else if (!output_compute(stoptime, true, wall() - t0, &nextoutput)) {
+      return false;
     }
-    if (!output_compute(stoptime, true, wall() - t0, &nextoutput)) return false;
   } else {
     // rejection KMC: dt_rkmc = nloop * dt_sweep per pass over all sets
     // (src/app_lattice.cpp:398-420)
@@ -1022,7 +1032,17 @@ bool Driver::command(std::vector<std::string> &w) {
   } else if (c == "read_sites") {
     if (w.size() != 2) return fail("Illegal read_sites command");
     return read_sites(w[1]);
-  } else if (c == "echo" || c == "log" || c == "reset_time" || c == "shell") {
+  } else if (c == "log") {
+    // Input::log (src/input.cpp:663-690): a new log file, or none
+    if (w.size() != 2) return fail("Illegal log command");
+    if (logfile) fclose(logfile);
+    logfile = nullptr;
+    if (w[1] != "none") {
+      logfile = fopen(w[1].c_str(), "w");
+      if (!logfile) return fail("Cannot open logfile " + w[1]);
+      fprintf(logfile, "SPPARKS (GB300 driver) -- continued logfile from same input script\n");
+    }
+  } else if (c == "echo" || c == "reset_time" || c == "shell") {
     print("WARNING: %s is ignored by the GPU driver\n", c.c_str());
   } else {
     return fail("Unknown command: " + c);

@@ -164,6 +164,12 @@ __global__ void kmc_sum64_kernel(KmcArgs a, double *chain_sum, int iset, int fp6
   }
 }
 
+// the root (total propensity) of every chain's tree, gathered
+__global__ void kmc_roots_kernel(KmcArgs a, int nchains, double *out) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nchains; c += gridDim.x * blockDim.x)
+    out[c] = a.trees[a.c_tree_off[c]];
+}
+
 // max over the chains of sector iset (all chains for iset < 0) of
 // sum/num_active, into *bits (non-negative doubles order as their bits)
 __global__ void kmc_pmax64_kernel(KmcArgs a, const double *chain_sum, int iset, int nt, unsigned long long *bits) {
@@ -372,6 +378,7 @@ struct KmcState {
   std::vector<int32_t> h_nactive;
   // FP32 runs with the FP64 shadow (fp64 == 0): per-chain FP64 sums
   int shadow = 0;
+  int in_run = 0;             // a run paused at an output time can continue
   double *d_sum64 = nullptr;
   double dt_rel_err = 0.0;    // max relative error of dt_kmc = nstop/pmax against FP64, last run
 };
@@ -520,6 +527,19 @@ static cudaError_t kmc_shadow64(spkgpu_lattice *h, const KmcArgs &a, int iset, i
   kmc_pmax64_kernel<<<(nt + 255) / 256, 256, 0, h->stream>>>(a, k->d_sum64, iset, nt, k->d_scalars + 2);
   h->launches += 2;
   return cudaGetLastError();
+}
+
+// the chains' roots in chain order (through the shadow buffer as scratch)
+static int kmc_roots(spkgpu_lattice *h, const KmcArgs &a, std::vector<double> &roots) {
+  KmcState *k = h->kmc;
+  roots.resize(k->nchains);
+  kmc_roots_kernel<<<(k->nchains + 255) / 256, 256, 0, h->stream>>>(a, k->nchains, k->d_sum64);
+  h->launches++;
+  KMC_CUDA(h, cudaGetLastError());
+  KMC_CUDA(h, cudaMemcpyAsync(roots.data(), k->d_sum64, k->nchains * sizeof(double), cudaMemcpyDeviceToHost,
+                              h->stream));
+  KMC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return SPKGPU_OK;
 }
 
 // the shadow's pmax (as max-ed since the last clear) and the sum of the
@@ -684,40 +704,19 @@ static int kmc_pmax(spkgpu_lattice *h, double *pmax) {
   return SPKGPU_OK;
 }
 
-extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime, spkgpu_kmc_stats *out) {
+extern "C" int spkgpu_kmc_run_until(spkgpu_lattice *h, double *ptime, double stoptime, double until, int32_t first,
+                                    spkgpu_kmc_stats *out) {
   if (!h || !ptime) return SPKGPU_ERR_ARG;
   KmcState *k = h->kmc;
   if (!k || !k->ready) return spk_fail(h, SPKGPU_ERR_STATE, "spkgpu_kmc_setup has not been called");
   if (!h->have_temperature) return spk_fail(h, SPKGPU_ERR_STATE, "temperature has not been set");
+  if (!first && !k->in_run) return spk_fail(h, SPKGPU_ERR_STATE, "no KMC run to continue");
   const int nsec = h->d.nsector;
   double time = *ptime;
   KmcArgs a = kmc_args(h);
-  // setup(): every propensity, every tree (src/app_lattice.cpp:340-347)
-  KMC_CUDA(h, kmc_launch(h, 0, a, nullptr, h->n, 0));
-  kmc_build_kernel<<<k->nchains, 256, 0, h->stream>>>(a, -1);
-  h->launches++;
-  KMC_CUDA(h, cudaGetLastError());
-  if (k->tstop > 0.0 && !k->adapt) k->dt_kmc = k->tstop;
-  if (k->adapt) {
-    // max over sets of sum/num_active (src/app_lattice.cpp:356-371)
-    std::vector<int32_t> nact(k->nchains);
-    std::vector<int64_t> toff(k->nchains + 1);
-    KMC_CUDA(h, cudaMemcpyAsync(nact.data(), k->d_nactive, k->nchains * 4, cudaMemcpyDeviceToHost, h->stream));
-    KMC_CUDA(h, cudaMemcpyAsync(toff.data(), k->d_tree_off, (k->nchains + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
-    KMC_CUDA(h, cudaStreamSynchronize(h->stream));
-    double pmax = 0.0;
-    for (int c = 0; c < k->nchains; c++) {
-      if (nact[c] <= 0) continue;
-      double root = 0.0;
-      KMC_CUDA(h, cudaMemcpy(&root, k->d_trees + toff[c], 8, cudaMemcpyDeviceToHost));
-      pmax = std::max(pmax, root / nact[c]);
-    }
-    k->dt_kmc = (pmax > 0.0) ? k->nstop / pmax : stoptime - time;
-  }
   // FP32 propensities with the FP64 shadow: pmax of the same chains at the
   // same moments from all-FP64 propensities, and the relative error of the
   // adaptive time step nstop/pmax it gives
-  k->dt_rel_err = 0.0;
   auto shadow_err = [&](double pmax32) -> int {
     double pmax64 = 0.0, tot64 = 0.0;
     int rc = kmc_shadow_read(h, &pmax64, &tot64);
@@ -730,13 +729,35 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
     cudaError_t e = cudaMemsetAsync(k->d_sum64, 0, k->nchains * sizeof(double), h->stream);
     return e == cudaSuccess ? cudaMemsetAsync(k->d_scalars + 2, 0, 8, h->stream) : e;
   };
-  if (k->shadow && k->adapt) {
-    KMC_CUDA(h, shadow_clear());
-    KMC_CUDA(h, kmc_shadow64(h, a, -1));
-    int rc = shadow_err(k->nstop / k->dt_kmc);
-    if (rc) return rc;
+  if (first) {
+    // setup(): every propensity, every tree (src/app_lattice.cpp:340-347)
+    KMC_CUDA(h, kmc_launch(h, 0, a, nullptr, h->n, 0));
+    kmc_build_kernel<<<k->nchains, 256, 0, h->stream>>>(a, -1);
+    h->launches++;
+    KMC_CUDA(h, cudaGetLastError());
+    if (k->tstop > 0.0 && !k->adapt) k->dt_kmc = k->tstop;
+    if (k->adapt) {
+      // max over sets of sum/num_active (src/app_lattice.cpp:356-371)
+      std::vector<double> roots;
+      std::vector<int32_t> nact(k->nchains);
+      int rc = kmc_roots(h, a, roots);
+      if (rc) return rc;
+      KMC_CUDA(h, cudaMemcpy(nact.data(), k->d_nactive, k->nchains * 4, cudaMemcpyDeviceToHost));
+      double pmax = 0.0;
+      for (int c = 0; c < k->nchains; c++)
+        if (nact[c] > 0) pmax = std::max(pmax, roots[c] / nact[c]);
+      k->dt_kmc = (pmax > 0.0) ? k->nstop / pmax : stoptime - time;
+    }
+    k->dt_rel_err = 0.0;
+    if (k->shadow && k->adapt) {
+      KMC_CUDA(h, shadow_clear());
+      KMC_CUDA(h, kmc_shadow64(h, a, -1));
+      int rc = shadow_err(k->nstop / k->dt_kmc);
+      if (rc) return rc;
+    }
+    k->dt_kmc = std::min(k->dt_kmc, stoptime - time);
+    k->in_run = 1;
   }
-  k->dt_kmc = std::min(k->dt_kmc, stoptime - time);
   if (stoptime > time) {
     bool alldone = false;
     while (!alldone) {
@@ -767,21 +788,21 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
         k->dt_kmc = (pmax > 0.0) ? k->nstop / pmax : stoptime - time;
         k->dt_kmc = std::min(k->dt_kmc, stoptime - time);
       }
+      // an output time: return to the caller, which continues the run
+      // with first = 0 (src/app_lattice.cpp:606-609)
+      if (!alldone && time >= until) break;
     }
   }
+  if (time >= stoptime) k->in_run = 0;
   *ptime = time;
   if (out) {
     unsigned long long na = 0;
     KMC_CUDA(h, cudaMemcpyAsync(&na, k->d_scalars + 1, 8, cudaMemcpyDeviceToHost, h->stream));
-    KMC_CUDA(h, cudaStreamSynchronize(h->stream));
-    std::vector<int64_t> toff(k->nchains + 1);
-    KMC_CUDA(h, cudaMemcpy(toff.data(), k->d_tree_off, (k->nchains + 1) * 8, cudaMemcpyDeviceToHost));
+    std::vector<double> roots;
+    int rc = kmc_roots(h, a, roots);
+    if (rc) return rc;
     double total = 0.0;
-    for (int c = 0; c < k->nchains; c++) {
-      double root = 0.0;
-      KMC_CUDA(h, cudaMemcpy(&root, k->d_trees + toff[c], 8, cudaMemcpyDeviceToHost));
-      total += root;
-    }
+    for (double r : roots) total += r;
     out->time = time;
     out->naccept = (int64_t)na;
     out->npass = k->npass;
@@ -795,7 +816,7 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
       double pm = 0.0, tot32 = 0.0, tot64 = 0.0;
       KMC_CUDA(h, shadow_clear());
       KMC_CUDA(h, kmc_shadow64(h, a, -1, 0));
-      int rc = kmc_shadow_read(h, &pm, &tot32);
+      rc = kmc_shadow_read(h, &pm, &tot32);
       if (rc) return rc;
       KMC_CUDA(h, shadow_clear());
       KMC_CUDA(h, kmc_shadow64(h, a, -1, 1));
@@ -806,4 +827,8 @@ extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime,
     }
   }
   return SPKGPU_OK;
+}
+
+extern "C" int spkgpu_kmc_run(spkgpu_lattice *h, double *ptime, double stoptime, spkgpu_kmc_stats *out) {
+  return spkgpu_kmc_run_until(h, ptime, stoptime, stoptime, 1, out);
 }

@@ -156,6 +156,21 @@ KMC_CASES = [
          temperature=0.8, seed=33, runs=[0.6]),
 ]
 
+# tree KMC with stats and energy between passes (Philox shim): the log's rows
+KMC_LOG_CASES = [
+    dict(name="kmclog_potts_sq8n_16_Q10", app="potts", nspins=10, lattice="sq/8n", nx=16, ny=16, nz=1,
+         temperature=1.0, seed=41, runs=[1.0, 0.5], stats=0.2),
+    dict(name="kmclog_ising_sc6n_8", app="ising", nspins=2, lattice="sc/6n", nx=8, ny=8, nz=8,
+         temperature=3.0, seed=42, runs=[0.6], stats=0.1),
+]
+
+
+def kmc_log_script(case):
+    lines = kmc_script(case)
+    k = lines.index("solve_style tree")
+    return ["log kmc.log"] + lines[:k] + ["diag_style energy", f"stats {case['stats']!r}"] + lines[k:]
+
+
 STRICT_CASES = [
     dict(name="strict_ising_sq4n_16", app="ising", nspins=2, lattice="sq/4n", nx=16, ny=16, nz=1,
          temperature=2.269, master_seed=56789, nruns=3, sweeps_per_run=4),
@@ -352,6 +367,22 @@ def main():
         header, rows = spk_serial_table(serial, case["lines"])
         fixtures["diag_logs"].append({"case": case, "header": header, "rows": rows})
         print("diag log case", case["name"], header, len(rows), "rows")
+    fixtures["kmc_logs"] = []
+    for case in KMC_LOG_CASES:
+        lines = kmc_log_script(case)
+        res = run_runner(philox, lines)
+        log = ROOT / "oracle" / "_ref" / "kmc.log"
+        header, rows = None, []
+        for line in log.read_text().splitlines():
+            p = line.split()
+            if p[:4] == ["Time", "Naccept", "Nreject", "Nsweeps"]:
+                header = p
+                continue
+            if header is not None and len(p) == len(header) and p[0][0].isdigit():
+                rows.append(p[:4] + ["-"] + p[5:])
+        log.unlink()
+        fixtures["kmc_logs"].append({"case": case, "script": lines, "header": header, "rows": rows, **res})
+        print("kmc log case", case["name"], len(rows), "rows")
     fixtures["io"] = []
     for case in IO_CASES:
         header, rows, files = spk_serial_io(serial, case)

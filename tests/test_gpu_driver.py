@@ -141,3 +141,29 @@ def test_dumps_and_read_sites_match_reference(sg, ref_fixtures, k, tmp_path, mon
     assert [drop_cpu(r) for r in rows] == [drop_cpu(r) for r in fx["rows"]]
     for name, text in fx["files"].items():
         assert (tmp_path / name).read_text() == text, name
+
+
+@pytest.mark.parametrize("k", range(2))
+def test_kmc_stats_between_passes_match_reference_log(sg, ref_fixtures, k, tmp_path, monkeypatch):
+    """tree KMC with `stats` and `diag_style energy`: the rows the reference
+    (Philox shim) prints between passes, from runs paused at each output
+    time (spkgpu_kmc_run_until) and continued."""
+    fx = ref_fixtures["kmc_logs"][k]
+    monkeypatch.chdir(tmp_path)
+    spk = sg.SPPARKS(cmdargs=["-screen", "none", "-log", "none"])
+    for line in fx["script"]:
+        if line.startswith("#!"):
+            if line.startswith("#! snap init"):
+                spk.set_sites(fx["snaps"]["init"]["spins"])
+            elif line.startswith("#! snap"):
+                tag = line.split()[2]
+                assert spk.sites().tolist() == fx["snaps"][tag]["spins"], tag
+            continue
+        if line.startswith("seed "):
+            line = f"seed {fx['case']['seed']}"
+        spk.command(line)
+    spk.close()
+    header, rows = stats_table((tmp_path / "kmc.log").read_text())
+    assert header == fx["header"]
+    drop_cpu = lambda r: r[:4] + r[5:]  # noqa: E731
+    assert [drop_cpu(r) for r in rows] == [drop_cpu(r) for r in fx["rows"]]

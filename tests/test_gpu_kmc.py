@@ -112,3 +112,29 @@ def test_kmc_fp32_run_states_its_error_against_fp64(sg):
             assert 0.0 < st["dt_rel_err"] < 1e-6
             assert 0.0 < st["prop_rel_err"] < 1e-6
         lat.close()
+
+
+def test_kmc_run_in_pieces_equals_one_run(sg):
+    """a run paused at arbitrary output times and continued ends in the same
+    state as one uninterrupted run"""
+    seed, nx = 51, 32
+    spin = oracle.init_spins(seed, nx * nx, 1, 12)
+    finals = []
+    for pieces in ([], [0.1, 0.35, 0.36, 0.9]):
+        lat = sg.Lattice("sq/8n", nx, nx, 1, "potts", 12, nsector=4, procs=(2, 2, 1), seed=seed)
+        lat.set_temperature(0.9)
+        lat.upload(spin)
+        lat.kmc_setup(fp64=True, nstop=0.25)
+        t, first, npieces = 0.0, True, 0
+        for until in pieces + [1.5]:
+            if t >= 1.5:
+                break  # the run is over: nothing to continue
+            st = lat.kmc_run(t, 1.5, until=max(until, t), first=first)
+            first = False
+            npieces += 1
+            assert st["time"] >= until or st["time"] >= 1.5
+            t = st["time"]
+        assert npieces > 1 or not pieces
+        finals.append((st["naccept"], st["npass"], st["time"], lat.download().tolist()))
+        lat.close()
+    assert finals[0] == finals[1]
