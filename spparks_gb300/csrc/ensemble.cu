@@ -799,9 +799,16 @@ int spkgpu_ensemble_upload(spkgpu_ensemble *e, const int32_t *spin, int64_t n) {
   if (!e || !spin) return SPKGPU_ERR_ARG;
   if (n != e->nsites) return ens_fail(e, SPKGPU_ERR_ARG, "site count mismatch");
   const int64_t chunk = (int64_t)1 << 24;
-  if (!e->d_stage) ENS_CUDA(e, cudaMalloc(&e->d_stage, (size_t)std::min(chunk, n) * 4));
   ENS_CUDA(e, cudaMemsetAsync(e->d_bad, 0, sizeof(int), e->stream));
-  for (int64_t off = 0; off < n; off += chunk) {
+  // registered pinned host memory: the conversion kernel reads it directly
+  const int32_t *mapped = (const int32_t *)mapped_host_ptr(spin);
+  if (mapped) {
+    ENS_CUDA(e, launch_convert_in(1, mapped, (int8_t *)e->buf[e->parity], n, e->d.nspins, e->d_bad, e->stream));
+    e->launches++;
+  } else if (!e->d_stage) {
+    ENS_CUDA(e, cudaMalloc(&e->d_stage, (size_t)std::min(chunk, n) * 4));
+  }
+  for (int64_t off = 0; !mapped && off < n; off += chunk) {
     int64_t m = std::min(chunk, n - off);
     ENS_CUDA(e, cudaMemcpyAsync(e->d_stage, spin + off, (size_t)m * 4, cudaMemcpyHostToDevice, e->stream));
     ENS_CUDA(e, launch_convert_in(1, e->d_stage, (int8_t *)e->buf[e->parity] + off, m, e->d.nspins, e->d_bad,
@@ -819,6 +826,14 @@ int spkgpu_ensemble_download(spkgpu_ensemble *e, int32_t *spin, int64_t n) {
   if (!e || !spin) return SPKGPU_ERR_ARG;
   if (n != e->nsites) return ens_fail(e, SPKGPU_ERR_ARG, "site count mismatch");
   const int64_t chunk = (int64_t)1 << 24;
+  // registered pinned host memory: the conversion kernel writes it directly
+  int32_t *mapped = (int32_t *)mapped_host_ptr(spin);
+  if (mapped) {
+    ENS_CUDA(e, launch_convert_out(1, (const int8_t *)e->buf[e->parity], mapped, n, e->stream));
+    e->launches++;
+    ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+    return SPKGPU_OK;
+  }
   if (!e->d_stage) ENS_CUDA(e, cudaMalloc(&e->d_stage, (size_t)std::min(chunk, n) * 4));
   for (int64_t off = 0; off < n; off += chunk) {
     int64_t m = std::min(chunk, n - off);

@@ -92,6 +92,18 @@ cudaError_t launch_phase(int lattice, int app, int spin_bytes, const PhaseArgs &
 cudaError_t launch_mask_clear(int lattice, const MaskClearArgs &a, cudaStream_t s, int num_sms);
 cudaError_t launch_energy(int lattice, int spin_bytes, const void *spin, int nx, int ny, int nz,
                           unsigned long long *out, cudaStream_t s, int num_sms);
+// The device address of host memory that kernels may read and write
+// directly (page-locked and registered with CUDA: cudaHostAlloc,
+// cudaMallocHost, cudaHostRegister), or nullptr for any other pointer.
+inline void *mapped_host_ptr(const void *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (at.type == cudaMemoryTypeHost && at.devicePointer) ? at.devicePointer : nullptr;
+}
+
 cudaError_t launch_convert_in(int spin_bytes, const int32_t *src, void *dst, int64_t n, int nspins,
                               int *bad, cudaStream_t s);
 cudaError_t launch_convert_out(int spin_bytes, const void *src, int32_t *dst, int64_t n,

@@ -297,11 +297,21 @@ static const int64_t kStageChunk = (int64_t)1 << 24;  // 16 Mi sites (64 MiB) pe
 int spkgpu_upload_spins(spkgpu_lattice *h, const int32_t *spin, int64_t n) {
   if (!h || !spin) return SPKGPU_ERR_ARG;
   if (n != h->n) return spk_fail(h, SPKGPU_ERR_ARG, "site count mismatch");
-  int rc = ensure_stage(h, std::min(n, kStageChunk) + 1);
-  if (rc) return rc;
   int *bad = (int *)(h->d_counters + 2);
   SPK_CUDA(h, cudaMemsetAsync(bad, 0, sizeof(int), h->stream));
-  for (int64_t off = 0; off < n; off += kStageChunk) {
+  // registered pinned host memory: the conversion kernel reads it directly
+  // (one pass over NVLink-C2C or PCIe, no staging copy)
+  const int32_t *mapped = (const int32_t *)spk::mapped_host_ptr(spin);
+  if (mapped) {
+    if (h->packed)
+      SPK_CUDA(h, spk::launch_packed_pack(mapped, (uint64_t *)h->d_spin, n / 64, bad, h->stream, h->num_sms));
+    else
+      SPK_CUDA(h, spk::launch_convert_in(h->spin_bytes, mapped, h->d_spin, n, h->d.nspins, bad, h->stream));
+    h->launches++;
+  }
+  int rc = mapped ? SPKGPU_OK : ensure_stage(h, std::min(n, kStageChunk) + 1);
+  if (rc) return rc;
+  for (int64_t off = 0; !mapped && off < n; off += kStageChunk) {
     int64_t m = std::min(kStageChunk, n - off);
     SPK_CUDA(h, cudaMemcpyAsync(h->d_stage, spin + off, (size_t)m * 4, cudaMemcpyHostToDevice, h->stream));
     if (h->packed)
@@ -333,6 +343,17 @@ int spkgpu_init_spins(spkgpu_lattice *h, int32_t lo, int32_t hi) {
 int spkgpu_download_spins(spkgpu_lattice *h, int32_t *spin, int64_t n) {
   if (!h || !spin) return SPKGPU_ERR_ARG;
   if (n != h->n) return spk_fail(h, SPKGPU_ERR_ARG, "site count mismatch");
+  // registered pinned host memory: the conversion kernel writes it directly
+  int32_t *mapped = (int32_t *)spk::mapped_host_ptr(spin);
+  if (mapped) {
+    if (h->packed)
+      SPK_CUDA(h, spk::launch_packed_unpack((const uint64_t *)h->d_spin, mapped, n / 64, h->stream, h->num_sms));
+    else
+      SPK_CUDA(h, spk::launch_convert_out(h->spin_bytes, h->d_spin, mapped, n, h->stream));
+    h->launches++;
+    SPK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SPKGPU_OK;
+  }
   int rc = ensure_stage(h, std::min(n, kStageChunk) + 1);
   if (rc) return rc;
   for (int64_t off = 0; off < n; off += kStageChunk) {

@@ -253,29 +253,86 @@ __global__ void convert_out_kernel(const S *src, int32_t *dst, int64_t n) {
     dst[i] = (int32_t)src[i];
 }
 
+// four sites per step, with 16-byte accesses on the int32 side: the int32
+// side may be pinned host memory the kernel reads or writes directly
+template <typename S>
+__global__ void convert_in4_kernel(const int4 *src, S *dst, int64_t n4, int nspins, int *bad) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += (int64_t)gridDim.x * blockDim.x) {
+    const int4 v = src[q];
+    if (v.x < 1 || v.x > nspins || v.y < 1 || v.y > nspins || v.z < 1 || v.z > nspins || v.w < 1 || v.w > nspins)
+      *bad = 1;
+    if (sizeof(S) == 1) {
+      ((uint32_t *)dst)[q] = (uint32_t)(uint8_t)v.x | ((uint32_t)(uint8_t)v.y << 8) |
+                             ((uint32_t)(uint8_t)v.z << 16) | ((uint32_t)(uint8_t)v.w << 24);
+    } else if (sizeof(S) == 2) {
+      ((uint2 *)dst)[q] = make_uint2((uint32_t)(uint16_t)v.x | ((uint32_t)(uint16_t)v.y << 16),
+                                     (uint32_t)(uint16_t)v.z | ((uint32_t)(uint16_t)v.w << 16));
+    } else {
+      ((int4 *)dst)[q] = v;
+    }
+  }
+}
+
+template <typename S>
+__global__ void convert_out4_kernel(const S *src, int4 *dst, int64_t n4) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += (int64_t)gridDim.x * blockDim.x) {
+    const S *p = src + 4 * q;
+    dst[q] = make_int4((int)p[0], (int)p[1], (int)p[2], (int)p[3]);
+  }
+}
+
+static unsigned convert_blocks(int64_t items) {
+  int64_t b = (items + 255) / 256;
+  return (unsigned)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
+}
+
 cudaError_t launch_convert_in(int spin_bytes, const int32_t *src, void *dst, int64_t n, int nspins, int *bad,
                               cudaStream_t s) {
-  int64_t blocks = (n + 255) / 256;
-  if (blocks > 4096) blocks = 4096;
   if (n <= 0) return cudaSuccess;
-  switch (spin_bytes) {
-    case 1: convert_in_kernel<int8_t><<<(unsigned)blocks, 256, 0, s>>>(src, (int8_t *)dst, n, nspins, bad); break;
-    case 2: convert_in_kernel<int16_t><<<(unsigned)blocks, 256, 0, s>>>(src, (int16_t *)dst, n, nspins, bad); break;
-    case 4: convert_in_kernel<int32_t><<<(unsigned)blocks, 256, 0, s>>>(src, (int32_t *)dst, n, nspins, bad); break;
-    default: return cudaErrorInvalidValue;
+  if (spin_bytes != 1 && spin_bytes != 2 && spin_bytes != 4) return cudaErrorInvalidValue;
+  const int64_t n4 = (((uintptr_t)src & 15) == 0 && ((uintptr_t)dst & (4 * spin_bytes - 1)) == 0) ? n / 4 : 0;
+  if (n4) {
+    const int4 *s4 = (const int4 *)src;
+    switch (spin_bytes) {
+      case 1: convert_in4_kernel<int8_t><<<convert_blocks(n4), 256, 0, s>>>(s4, (int8_t *)dst, n4, nspins, bad); break;
+      case 2: convert_in4_kernel<int16_t><<<convert_blocks(n4), 256, 0, s>>>(s4, (int16_t *)dst, n4, nspins, bad); break;
+      case 4: convert_in4_kernel<int32_t><<<convert_blocks(n4), 256, 0, s>>>(s4, (int32_t *)dst, n4, nspins, bad); break;
+    }
+  }
+  const int64_t r0 = 4 * n4, nr = n - r0;
+  if (nr > 0) {
+    const int32_t *sr = src + r0;
+    char *dr = (char *)dst + r0 * spin_bytes;
+    switch (spin_bytes) {
+      case 1: convert_in_kernel<int8_t><<<convert_blocks(nr), 256, 0, s>>>(sr, (int8_t *)dr, nr, nspins, bad); break;
+      case 2: convert_in_kernel<int16_t><<<convert_blocks(nr), 256, 0, s>>>(sr, (int16_t *)dr, nr, nspins, bad); break;
+      case 4: convert_in_kernel<int32_t><<<convert_blocks(nr), 256, 0, s>>>(sr, (int32_t *)dr, nr, nspins, bad); break;
+    }
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_convert_out(int spin_bytes, const void *src, int32_t *dst, int64_t n, cudaStream_t s) {
-  int64_t blocks = (n + 255) / 256;
-  if (blocks > 4096) blocks = 4096;
   if (n <= 0) return cudaSuccess;
-  switch (spin_bytes) {
-    case 1: convert_out_kernel<int8_t><<<(unsigned)blocks, 256, 0, s>>>((const int8_t *)src, dst, n); break;
-    case 2: convert_out_kernel<int16_t><<<(unsigned)blocks, 256, 0, s>>>((const int16_t *)src, dst, n); break;
-    case 4: convert_out_kernel<int32_t><<<(unsigned)blocks, 256, 0, s>>>((const int32_t *)src, dst, n); break;
-    default: return cudaErrorInvalidValue;
+  if (spin_bytes != 1 && spin_bytes != 2 && spin_bytes != 4) return cudaErrorInvalidValue;
+  const int64_t n4 = (((uintptr_t)dst & 15) == 0 && ((uintptr_t)src & (4 * spin_bytes - 1)) == 0) ? n / 4 : 0;
+  if (n4) {
+    int4 *d4 = (int4 *)dst;
+    switch (spin_bytes) {
+      case 1: convert_out4_kernel<int8_t><<<convert_blocks(n4), 256, 0, s>>>((const int8_t *)src, d4, n4); break;
+      case 2: convert_out4_kernel<int16_t><<<convert_blocks(n4), 256, 0, s>>>((const int16_t *)src, d4, n4); break;
+      case 4: convert_out4_kernel<int32_t><<<convert_blocks(n4), 256, 0, s>>>((const int32_t *)src, d4, n4); break;
+    }
+  }
+  const int64_t r0 = 4 * n4, nr = n - r0;
+  if (nr > 0) {
+    const char *sr = (const char *)src + r0 * spin_bytes;
+    int32_t *dr = dst + r0;
+    switch (spin_bytes) {
+      case 1: convert_out_kernel<int8_t><<<convert_blocks(nr), 256, 0, s>>>((const int8_t *)sr, dr, nr); break;
+      case 2: convert_out_kernel<int16_t><<<convert_blocks(nr), 256, 0, s>>>((const int16_t *)sr, dr, nr); break;
+      case 4: convert_out_kernel<int32_t><<<convert_blocks(nr), 256, 0, s>>>((const int32_t *)sr, dr, nr); break;
+    }
   }
   return cudaGetLastError();
 }

@@ -159,3 +159,54 @@ def test_energy_matches_oracle(sg):
 def test_philox_rate_calibration(sg):
     """the draw-side ceiling the bench reports: Philox blocks/s of the device"""
     assert sg.philox_rate(0, 256) > 1e10
+
+
+@pytest.mark.parametrize("lattice,nx,ny,nz,sb", [("sq/4n", 64, 48, 1, 1), ("sq/8n", 30, 10, 1, 2),
+                                                 ("sc/26n", 6, 6, 6, 4), ("sc/6n", 64, 4, 4, -1),
+                                                 ("sq/4n", 10, 6, 1, 1)])
+def test_pinned_host_buffers_equal_pageable(sg, lattice, nx, ny, nz, sb):
+    """uploads and downloads through registered pinned host memory (read and
+    written by the conversion kernels directly) equal the staged path for
+    pageable memory, including the invalid-value check"""
+    import torch
+
+    app, q = ("ising", 2) if sb == -1 else ("potts", 9)
+    n = nx * ny * nz
+    spin = oracle.init_spins(77, n, 1, q)
+    pinned = torch.from_numpy(spin.copy()).pin_memory()
+    out_pinned = torch.zeros(n, dtype=torch.int32).pin_memory()
+    lat = sg.Lattice(lattice, nx, ny, nz, app, q, spin_bytes=sb, seed=5)
+    lat.set_temperature(0.8)
+    lat.upload(pinned.numpy())
+    lat.sweep(2)
+    lat.download(out_pinned.numpy())
+    ref = sg.Lattice(lattice, nx, ny, nz, app, q, spin_bytes=sb, seed=5)
+    ref.set_temperature(0.8)
+    ref.upload(spin)
+    ref.sweep(2)
+    assert out_pinned.numpy().tolist() == ref.download().tolist()
+    bad = pinned.clone().pin_memory()
+    bad[n - 1] = q + 1  # in the tail or the last 16-byte group
+    with pytest.raises(sg.SpkGpuError):
+        lat.upload(bad.numpy())
+    lat.close()
+    ref.close()
+
+
+def test_pinned_ensemble_buffers_equal_pageable(sg):
+    import torch
+
+    L, T = [32, 64, 96], [2.0, 2.4, 2.8]
+    n = sum(l * l for l in L)
+    spin = oracle.init_spins(9, n, 1, 2)
+    out = []
+    for pin in (False, True):
+        ens = sg.Ensemble(L, T, "ising", 2, seed=3, exchange_every=2)
+        src = torch.from_numpy(spin.copy()).pin_memory().numpy() if pin else spin
+        ens.upload(src)
+        ens.run(4)
+        dst = torch.zeros(n, dtype=torch.int32).pin_memory().numpy() if pin else np.zeros(n, dtype=np.int32)
+        ens.download(dst)
+        out.append(dst.tolist())
+        ens.close()
+    assert out[0] == out[1]
