@@ -398,11 +398,11 @@ class Ensemble:
         """Execution form the autotuner kept ("persistent" or "launches") and
         its time of one step in each form (ms, None where not timed)."""
         m = ctypes.c_int32()
-        ms = (ctypes.c_float * 2)()
+        names = ("persistent", "launches", "launches2", "launches4")
+        ms = (ctypes.c_float * len(names))()
         self._check(self.lib.spkgpu_ensemble_mode(self.h, ctypes.byref(m), ms))
-        names = ("persistent", "launches")
         return {"mode": names[m.value],
-                "tune_ms": {names[k]: (float(ms[k]) if ms[k] >= 0 else None) for k in range(2)}}
+                "tune_ms": {names[k]: (float(ms[k]) if ms[k] >= 0 else None) for k in range(len(names))}}
 
     def sweep_kernel_ms(self):
         """(ms, launches): device time of the sweep kernels in the last replay

@@ -330,18 +330,13 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
 // replayed; ensemble_advance_kernel then moves ctl on by m sweeps.  Bonds and
 // the exchange round run as their own launches between the last sweep of a
 // period and the advance.
-template <int APP, typename S>
-__global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) ensemble_sweep_kernel(EnsArgs a,
-                                                                                                     int k) {
-  __shared__ __align__(16) S stage[kStageSites];
-  __shared__ uint64_t thr[5];
-  const int2 tp = a.tile_pos[blockIdx.x];
+// the job of tile t in sweep k of the launch-per-sweep form
+template <typename S>
+__device__ __forceinline__ void sweep_job(const EnsArgs &a, int t, int parity, uint32_t sweep, TileJob &j) {
+  const int2 tp = a.tile_pos[t];
   const int r = tp.x;
   const int L = a.L[r];
-  const int parity = *(volatile int *)&a.ctl->parity ^ (k & 1);
   const int64_t base = a.base[r];
-  const int tix = a.tidx[r];
-  TileJob j;
   j.src = (const S *)(parity ? a.buf1 : a.buf0) + base;
   j.dst = (S *)(parity ? a.buf0 : a.buf1) + base;
   j.L = L;
@@ -351,17 +346,69 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) e
   j.base = 0;  // replicas differ by Philox stream word; site counter is local
   j.seed = a.seed;
   j.key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
-  j.sweep = *(volatile uint32_t *)&a.ctl->sweep + (uint32_t)k;
+  j.sweep = sweep;
   j.nspins = a.nspins;
-  j.replica = tix;
-  if (threadIdx.x < 5) thr[threadIdx.x] = a.thr[(int64_t)tix * 5 + threadIdx.x];
-  tile_stage_async<S>(j, stage);
-  cp_async_commit();
+  j.replica = a.tidx[r];
+}
+
+// TPC consecutive tiles per CTA: tile t+1 is staged (cp.async) into the
+// next of three buffers while tile t is swept; a buffer is staged again
+// only after every thread has passed the barrier of the tile in between.
+// Change counts go from each warp to a spread counter slot (no block barrier).
+template <int APP, typename S, int TPC>
+__global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) ensemble_sweep_kernel(EnsArgs a,
+                                                                                                     int k) {
+  constexpr int NB = TPC > 1 ? 3 : 1;
+  __shared__ __align__(16) S stage[NB][kStageSites];
+  __shared__ uint64_t thr[NB][5];
+  const int parity = *(volatile int *)&a.ctl->parity ^ (k & 1);
+  const uint32_t sweep = *(volatile uint32_t *)&a.ctl->sweep + (uint32_t)k;
+  unsigned int changed = 0;
+  if constexpr (TPC == 1) {
+    TileJob j;
+    sweep_job<S>(a, blockIdx.x, parity, sweep, j);
+    if (threadIdx.x < 5) thr[0][threadIdx.x] = a.thr[(int64_t)j.replica * 5 + threadIdx.x];
+    tile_stage_async<S>(j, stage[0]);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    j.thr = thr[0];
+    changed = (unsigned int)tile_sweep_sq4<APP, S>(j, stage[0]);
+  } else {
+    const int t0 = blockIdx.x * TPC;
+    const int t1 = min(t0 + TPC, a.ntiles);
+    {
+      TileJob j;
+      sweep_job<S>(a, t0, parity, sweep, j);
+      if (threadIdx.x < 5) thr[0][threadIdx.x] = a.thr[(int64_t)j.replica * 5 + threadIdx.x];
+      tile_stage_async<S>(j, stage[0]);
+      cp_async_commit();
+    }
+    int b = 0;
+    for (int t = t0; t < t1; t++) {
+      const int bn = (b + 1 == NB) ? 0 : b + 1;
+      if (t + 1 < t1) {
+        TileJob nj;
+        sweep_job<S>(a, t + 1, parity, sweep, nj);
+        if (threadIdx.x < 5) thr[bn][threadIdx.x] = a.thr[(int64_t)nj.replica * 5 + threadIdx.x];
+        tile_stage_async<S>(nj, stage[bn]);
+      }
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+      // the job is rebuilt from the tables rather than carried across tiles
+      TileJob j;
+      sweep_job<S>(a, t, parity, sweep, j);
+      j.thr = thr[b];
+      changed += (unsigned int)tile_sweep_sq4<APP, S>(j, stage[b]);
+      b = bn;
+    }
+  }
   cp_async_wait<0>();
-  __syncthreads();
-  j.thr = thr;
-  int changed = tile_sweep_sq4<APP, S>(j, stage);
-  block_count_add(a.nacc_slots, (unsigned long long)changed);
+  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, changed);
+  if ((threadIdx.x & 31) == 0 && w)
+    atomicAdd(&a.nacc_slots[(blockIdx.x * (kTileThreads / 32) + (threadIdx.x >> 5)) & (kCounterSlots - 1)],
+              (unsigned long long)w);
 }
 
 // unlike bonds of every replica in the buffer the sweep k-1 wrote
@@ -411,7 +458,7 @@ struct spkgpu_ensemble {
           *d_group_start = nullptr, *d_slot_t = nullptr, *d_slot_group = nullptr, *d_who = nullptr;
   unsigned long long *d_nacc_slots = nullptr;
   int mode = SPKGPU_ENSEMBLE_PERSISTENT;
-  float tune_ms[2] = {-1.0f, -1.0f};  // the autotuner's step times per mode
+  float tune_ms[SPKGPU_ENSEMBLE_NMODES] = {-1.0f, -1.0f, -1.0f, -1.0f};  // the autotuner's step times per mode
   int64_t enq = 0;  // sweeps enqueued so far (the host's copy of ctl->sweep)
   std::vector<int32_t> slot_init;  // replica in each exchange slot at creation
   int64_t *d_base = nullptr;
@@ -459,17 +506,27 @@ static cudaError_t ens_launch(spkgpu_ensemble *e, int nsweeps) {
   return cudaLaunchCooperativeKernel(e->kfn, dim3(e->grid), dim3(kTileThreads), params, 0, e->stream);
 }
 
+// one sweep launch of the per-sweep forms (1, 2 or 4 tiles per CTA)
+static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cudaStream_t st) {
+  const int tpc = e->mode == SPKGPU_ENSEMBLE_LAUNCHES4 ? 4 : (e->mode == SPKGPU_ENSEMBLE_LAUNCHES2 ? 2 : 1);
+  const unsigned grid = (unsigned)((e->ntiles + tpc - 1) / tpc);
+  if (e->d.app == SPKGPU_ISING) {
+    if (tpc == 4) ensemble_sweep_kernel<SPKGPU_ISING, int8_t, 4><<<grid, kTileThreads, 0, st>>>(a, k);
+    else if (tpc == 2) ensemble_sweep_kernel<SPKGPU_ISING, int8_t, 2><<<grid, kTileThreads, 0, st>>>(a, k);
+    else ensemble_sweep_kernel<SPKGPU_ISING, int8_t, 1><<<grid, kTileThreads, 0, st>>>(a, k);
+  } else {
+    if (tpc == 4) ensemble_sweep_kernel<SPKGPU_POTTS, int8_t, 4><<<grid, kTileThreads, 0, st>>>(a, k);
+    else if (tpc == 2) ensemble_sweep_kernel<SPKGPU_POTTS, int8_t, 2><<<grid, kTileThreads, 0, st>>>(a, k);
+    else ensemble_sweep_kernel<SPKGPU_POTTS, int8_t, 1><<<grid, kTileThreads, 0, st>>>(a, k);
+  }
+}
+
 // launch-per-sweep mode: m sweeps, the bonds and exchange round if `exchange`,
 // then the advance of ctl; returns the number of kernels through *nk
 static cudaError_t ens_launch_group(spkgpu_ensemble *e, int m, bool exchange, int64_t *nk) {
   const EnsArgs &a = e->args;
   const unsigned nt = (unsigned)e->ntiles;
-  for (int k = 0; k < m; k++) {
-    if (e->d.app == SPKGPU_ISING)
-      ensemble_sweep_kernel<SPKGPU_ISING, int8_t><<<nt, kTileThreads, 0, e->stream>>>(a, k);
-    else
-      ensemble_sweep_kernel<SPKGPU_POTTS, int8_t><<<nt, kTileThreads, 0, e->stream>>>(a, k);
-  }
+  for (int k = 0; k < m; k++) launch_sweep(e, a, k, e->stream);
   if (exchange) ensemble_bonds_kernel<int8_t><<<nt, kTileThreads, 0, e->stream>>>(a, m);
   ensemble_advance_kernel<<<1, 256, 0, e->stream>>>(a, m, exchange ? 1 : 0);
   *nk += m + (exchange ? 1 : 0) + 1;
@@ -505,12 +562,7 @@ static void ens_capture(spkgpu_ensemble *e) {
   } else {
     const EnsArgs &a = e->args;
     const unsigned nt = (unsigned)e->ntiles;
-    for (int k = 0; k < e->chunk; k++) {
-      if (e->d.app == SPKGPU_ISING)
-        ensemble_sweep_kernel<SPKGPU_ISING, int8_t><<<nt, kTileThreads, 0, cap>>>(a, k);
-      else
-        ensemble_sweep_kernel<SPKGPU_POTTS, int8_t><<<nt, kTileThreads, 0, cap>>>(a, k);
-    }
+    for (int k = 0; k < e->chunk; k++) launch_sweep(e, a, k, cap);
     kev = kev && cudaEventRecordWithFlags(e->kev1, cap, cudaEventRecordExternal) == cudaSuccess;
     const bool exchange = e->d.exchange_every > 0;
     if (exchange) ensemble_bonds_kernel<int8_t><<<nt, kTileThreads, 0, cap>>>(a, e->chunk);
@@ -558,11 +610,13 @@ static cudaError_t ens_reset(spkgpu_ensemble *e) {
 // (after a warm-up step, sites all 1) and keeps the faster; the choice is
 // cached per (app, replicas, tiles, exchange period) for the process.
 // SPKGPU_ENSEMBLE_MODE=persistent|launches forces a mode.
+static const char *const kModeNames[SPKGPU_ENSEMBLE_NMODES] = {"persistent", "launches", "launches2", "launches4"};
+
 static int ens_pick_mode(spkgpu_ensemble *e, float *ms_out) {
-  ms_out[0] = ms_out[1] = -1.0f;
+  for (int m = 0; m < SPKGPU_ENSEMBLE_NMODES; m++) ms_out[m] = -1.0f;
   if (const char *env = getenv("SPKGPU_ENSEMBLE_MODE")) {
-    if (!strcmp(env, "persistent")) return SPKGPU_ENSEMBLE_PERSISTENT;
-    if (!strcmp(env, "launches")) return SPKGPU_ENSEMBLE_LAUNCHES;
+    for (int m = 0; m < SPKGPU_ENSEMBLE_NMODES; m++)
+      if (!strcmp(env, kModeNames[m])) return m;
   }
   static std::mutex mu;
   static std::map<std::vector<int64_t>, int> cache;
@@ -574,7 +628,7 @@ static int ens_pick_mode(spkgpu_ensemble *e, float *ms_out) {
   }
   int best = SPKGPU_ENSEMBLE_PERSISTENT;
   float best_ms = -1.0f;
-  for (int mode : {SPKGPU_ENSEMBLE_PERSISTENT, SPKGPU_ENSEMBLE_LAUNCHES}) {
+  for (int mode = 0; mode < SPKGPU_ENSEMBLE_NMODES; mode++) {
     e->mode = mode;
     ens_capture(e);
     if (!e->gexec) continue;
@@ -957,10 +1011,8 @@ int spkgpu_ensemble_sweep_kernel_ms(spkgpu_ensemble *e, float *ms, int32_t *nlau
 int spkgpu_ensemble_mode(const spkgpu_ensemble *e, int32_t *mode, float *tune_ms) {
   if (!e || !mode) return SPKGPU_ERR_ARG;
   *mode = e->mode;
-  if (tune_ms) {
-    tune_ms[0] = e->tune_ms[0];
-    tune_ms[1] = e->tune_ms[1];
-  }
+  if (tune_ms)
+    for (int m = 0; m < SPKGPU_ENSEMBLE_NMODES; m++) tune_ms[m] = e->tune_ms[m];
   return SPKGPU_OK;
 }
 

@@ -49,7 +49,7 @@ def ensemble_case(seed=777):
     return L, T, spins
 
 
-@pytest.fixture(params=["persistent", "launches"])
+@pytest.fixture(params=["persistent", "launches", "launches2", "launches4"])
 def mode(request, monkeypatch):
     """both execution forms of the ensemble, forced past the autotuner"""
     monkeypatch.setenv("SPKGPU_ENSEMBLE_MODE", request.param)
