@@ -342,7 +342,7 @@ def run_ours(args):
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     traffic, traffic_src = profile_traffic(kname)
     # the draw-side ceiling: one Philox4x32-10 block per x-pair of sites
-    philox_bps = sg.philox_rate(device)
+    philox_bps = sg.philox_rate(device, 1024)
 
     if rank != 0:
         return

@@ -34,8 +34,12 @@ __global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
-  int changed = tile_sweep_sq4<APP, S>(j, stage);
-  block_count_add(a.naccept, (unsigned long long)changed);
+  const unsigned int changed = (unsigned int)tile_sweep_sq4<APP, S>(j, stage);
+  // each warp adds its count to a spread slot (no block barrier)
+  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, changed);
+  if ((threadIdx.x & 31) == 0 && w)
+    atomicAdd(&a.naccept[(blockIdx.x * (kTileThreads / 32) + (threadIdx.x >> 5)) & (kCounterSlots - 1)],
+              (unsigned long long)w);
 }
 
 bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny) {
