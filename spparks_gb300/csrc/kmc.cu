@@ -253,13 +253,30 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
   }
   double timesector = 0.0;
   unsigned int done_events = 0;
+  // the draws of the next 32 events, one per lane: the Philox block's pick
+  // and event words and the clock's log(u), computed in one pass (the FP64
+  // log is the costliest step of an event on this GPU)
+  uint32_t pre_x = 0, pre_z = 0;
+  double pre_log = 0.0;
+  int pre_left = 0;
   while (sum != 0.0) {
-    U4 w = kmc_block(a.seed, (uint32_t)c, k);
+    if (pre_left == 0) {
+      const U4 pw = kmc_block(a.seed, (uint32_t)c, k + (unsigned long long)lane);
+      pre_x = pw.x;
+      pre_z = pw.z;
+      pre_log = log(word_to_uniform(pw.y));
+      pre_left = 32;
+    }
+    const int slot = 32 - pre_left;
+    pre_left--;
+    const uint32_t wx = __shfl_sync(0xFFFFFFFFu, pre_x, slot);
+    const uint32_t wz = __shfl_sync(0xFFFFFFFFu, pre_z, slot);
+    const double lu = __shfl_sync(0xFFFFFFFFu, pre_log, slot);
     k++;
     int m = 0;
-    if (lane == 0) m = tree_find(T, leaf0, word_to_uniform(w.x) * sum);
+    if (lane == 0) m = tree_find(T, leaf0, word_to_uniform(wx) * sum);
     m = __shfl_sync(0xFFFFFFFFu, m, 0);
-    double dt = -1.0 / sum * log(word_to_uniform(w.y));
+    double dt = -1.0 / sum * lu;
     timesector += dt;
     if (timesector >= a.dt_kmc) break;
     int64_t i = site2i[m];
@@ -273,7 +290,7 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
       } else {
         int nb[NN];
         load_neighbors<S, LAT>(spin, i, a.nx, a.ny, a.nz, nb);
-        double threshhold = word_to_uniform(w.z) * T[leaf0 + m];
+        double threshhold = word_to_uniform(wz) * T[leaf0 + m];
         int e0 = count_unlike<NN>(own, nb);
         uint32_t first = first_appearance<NN>(own, nb);
         int value = own;
@@ -322,8 +339,9 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
       double pj = __shfl_sync(0xFFFFFFFFu, p, j);
       if (lj < 0) continue;
       if (lane == 0) {
-        double old = T[leaf0 + lj];
-        nactive += (pj > 0.0) - (old > 0.0);
+        // propensities are >= 0: positive <=> non-zero bits
+        const double old = T[leaf0 + lj];
+        nactive += (__double_as_longlong(pj) != 0) - (__double_as_longlong(old) != 0);
         T[leaf0 + lj] = pj;
       }
       __syncwarp();
