@@ -210,13 +210,20 @@ __global__ void kmc_build_kernel(KmcArgs a, int iset) {
   }
 }
 
-// SolveTree::find (src/solve_tree.cpp:207-224)
+// a <= b for doubles that are both >= +0 (propensities, their sums, times):
+// their bit patterns order as integers, and an integer compare keeps the
+// scarce FP64 pipe for the arithmetic
+__device__ __forceinline__ bool nonneg_le(double a, double b) {
+  return __double_as_longlong(a) <= __double_as_longlong(b);
+}
+
+// SolveTree::find (src/solve_tree.cpp:207-224); value and the tree are >= 0
 __device__ __forceinline__ int tree_find(const double *T, int leaf0, double value) {
   int i = 0;
   while (i < leaf0) {
     int left = 2 * i + 1;
     double tl = T[left];
-    if (value <= tl) i = left;
+    if (nonneg_le(value, tl)) i = left;
     else {
       value -= tl;
       i = left + 1;
@@ -256,29 +263,28 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
   // the draws of the next 32 events, one per lane: the Philox block's pick
   // and event words and the clock's log(u), computed in one pass (the FP64
   // log is the costliest step of an event on this GPU)
-  uint32_t pre_x = 0, pre_z = 0;
-  double pre_log = 0.0;
+  double pre_ux = 0.0, pre_uz = 0.0, pre_log = 0.0;
   int pre_left = 0;
-  while (sum != 0.0) {
+  while (__double_as_longlong(sum) != 0) {  // sum >= 0
     if (pre_left == 0) {
       const U4 pw = kmc_block(a.seed, (uint32_t)c, k + (unsigned long long)lane);
-      pre_x = pw.x;
-      pre_z = pw.z;
+      pre_ux = word_to_uniform(pw.x);
+      pre_uz = word_to_uniform(pw.z);
       pre_log = log(word_to_uniform(pw.y));
       pre_left = 32;
     }
     const int slot = 32 - pre_left;
     pre_left--;
-    const uint32_t wx = __shfl_sync(0xFFFFFFFFu, pre_x, slot);
-    const uint32_t wz = __shfl_sync(0xFFFFFFFFu, pre_z, slot);
+    const double ux = __shfl_sync(0xFFFFFFFFu, pre_ux, slot);
+    const double uz = __shfl_sync(0xFFFFFFFFu, pre_uz, slot);
     const double lu = __shfl_sync(0xFFFFFFFFu, pre_log, slot);
     k++;
     int m = 0;
-    if (lane == 0) m = tree_find(T, leaf0, word_to_uniform(wx) * sum);
+    if (lane == 0) m = tree_find(T, leaf0, ux * sum);
     m = __shfl_sync(0xFFFFFFFFu, m, 0);
     double dt = -1.0 / sum * lu;
     timesector += dt;
-    if (timesector >= a.dt_kmc) break;
+    if (nonneg_le(a.dt_kmc, timesector)) break;  // timesector >= dt_kmc
     int64_t i = site2i[m];
     int x, y, z;
     site_coords<LAT>(i, a.nx, a.ny, x, y, z);
@@ -290,7 +296,7 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
       } else {
         int nb[NN];
         load_neighbors<S, LAT>(spin, i, a.nx, a.ny, a.nz, nb);
-        double threshhold = word_to_uniform(wz) * T[leaf0 + m];
+        double threshhold = uz * T[leaf0 + m];
         int e0 = count_unlike<NN>(own, nb);
         uint32_t first = first_appearance<NN>(own, nb);
         int value = own;
@@ -302,7 +308,7 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
             int e1 = count_unlike<NN>(value, nb);
             if (e1 <= e0) prob += 1.0;
             else if (!a.zero_t) prob += a.pexp[e1 - e0];
-            if (prob >= threshhold) break;
+            if (nonneg_le(threshhold, prob)) break;  // prob >= threshhold
           }
         } else {
           float prob = 0.0f;
@@ -312,7 +318,7 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
             int e1 = count_unlike<NN>(value, nb);
             if (e1 <= e0) prob += 1.0f;
             else if (!a.zero_t) prob += a.pexpf[e1 - e0];
-            if ((double)prob >= threshhold) break;
+            if (nonneg_le(threshhold, (double)prob)) break;
           }
         }
         spin[i] = (S)value;
