@@ -72,6 +72,11 @@ class KmcStats(ctypes.Structure):
                 ("prop_rel_err", ctypes.c_double), ("dt_rel_err", ctypes.c_double)]
 
 
+# execution forms of an ensemble, in the order of SPKGPU_ENSEMBLE_* (spkgpu.h);
+# "warps" (one tile per warp) exists for Ising only
+ENSEMBLE_MODES = ("persistent", "launches", "launches2", "launches4", "warps")
+
+
 class EnsembleDesc(ctypes.Structure):
     _fields_ = [
         ("nreplica", ctypes.c_int32),
@@ -395,10 +400,10 @@ class Ensemble:
                 "exchange_tries": s.exchange_tries, "exchange_accepts": s.exchange_accepts}
 
     def mode(self) -> dict:
-        """Execution form the autotuner kept ("persistent" or "launches") and
-        its time of one step in each form (ms, None where not timed)."""
+        """Execution form the autotuner kept (one of ENSEMBLE_MODES) and its
+        time of one step in each form (ms, None where not timed)."""
         m = ctypes.c_int32()
-        names = ("persistent", "launches", "launches2", "launches4")
+        names = ENSEMBLE_MODES
         ms = (ctypes.c_float * len(names))()
         self._check(self.lib.spkgpu_ensemble_mode(self.h, ctypes.byref(m), ms))
         return {"mode": names[m.value],

@@ -32,6 +32,7 @@
 #include "counters.cuh"
 #include "spk_internal.h"
 #include "tile_sweep.cuh"
+#include "warp_tile.cuh"
 
 namespace spk {
 
@@ -72,6 +73,9 @@ struct EnsArgs {
   uint32_t seed;
   EnsCtl *ctl;
   unsigned long long *nacc_slots;  // kCounterSlots change counters (launch-per-sweep mode)
+  const int32_t *pair_rep;      // warp form: replica of each CTA's tile pair
+  const int32_t *pair_tile;     // warp form: the pair's two tiles (-1: none)
+  int npairs;
 };
 
 constexpr long long kBarrierSpinLimit = 1LL << 25;  // ~seconds with nanosleep: then give up
@@ -411,6 +415,39 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) e
               (unsigned long long)w);
 }
 
+// Ising, warp form: CTA b sweeps the tiles pair_tile[2b] and pair_tile[2b+1]
+// of replica pair_rep[b], one per warp (warp_tile.cuh); no block barrier.
+__global__ void __launch_bounds__(64, 32) ensemble_warp_kernel(EnsArgs a, int k) {
+  __shared__ __align__(16) int8_t stage[2][kWStageBytes];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = a.pair_tile[2 * blockIdx.x + warp];
+  if (t < 0) return;
+  const int r = a.pair_rep[blockIdx.x];
+  const int parity = *(volatile int *)&a.ctl->parity ^ (k & 1);
+  const int L = a.L[r];
+  const int64_t base = a.base[r];
+  const int pos = a.tile_pos[t].y;
+  TileJob j;
+  j.src = (const int8_t *)(parity ? a.buf1 : a.buf0) + base;
+  j.dst = (int8_t *)(parity ? a.buf0 : a.buf1) + base;
+  j.L = L;
+  j.Ly = L;
+  j.x0 = (pos & 0xFFFF) * kTile;
+  j.y0 = (pos >> 16) * kTile;
+  j.base = 0;
+  j.seed = a.seed;
+  j.key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
+  j.sweep = *(volatile uint32_t *)&a.ctl->sweep + (uint32_t)k;
+  j.nspins = a.nspins;
+  j.replica = a.tidx[r];
+  j.thr = a.thr + (int64_t)j.replica * 5;
+  j.t2 = j.thr[2];
+  j.t4 = j.thr[4];
+  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8(j, stage[warp], lane));
+  if (lane == 0 && w)
+    atomicAdd(&a.nacc_slots[(2 * blockIdx.x + warp) & (kCounterSlots - 1)], (unsigned long long)w);
+}
+
 // unlike bonds of every replica in the buffer the sweep k-1 wrote
 template <typename S>
 __global__ void __launch_bounds__(kTileThreads) ensemble_bonds_kernel(EnsArgs a, int k) {
@@ -458,7 +495,9 @@ struct spkgpu_ensemble {
           *d_group_start = nullptr, *d_slot_t = nullptr, *d_slot_group = nullptr, *d_who = nullptr;
   unsigned long long *d_nacc_slots = nullptr;
   int mode = SPKGPU_ENSEMBLE_PERSISTENT;
-  float tune_ms[SPKGPU_ENSEMBLE_NMODES] = {-1.0f, -1.0f, -1.0f, -1.0f};  // the autotuner's step times per mode
+  float tune_ms[SPKGPU_ENSEMBLE_NMODES] = {-1.0f, -1.0f, -1.0f, -1.0f, -1.0f};  // the autotuner's step times per mode
+  int32_t *d_pair_rep = nullptr, *d_pair_tile = nullptr;
+  int npairs = 0;
   int64_t enq = 0;  // sweeps enqueued so far (the host's copy of ctl->sweep)
   std::vector<int32_t> slot_init;  // replica in each exchange slot at creation
   int64_t *d_base = nullptr;
@@ -508,6 +547,10 @@ static cudaError_t ens_launch(spkgpu_ensemble *e, int nsweeps) {
 
 // one sweep launch of the per-sweep forms (1, 2 or 4 tiles per CTA)
 static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cudaStream_t st) {
+  if (e->mode == SPKGPU_ENSEMBLE_WARPS) {
+    ensemble_warp_kernel<<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
+    return;
+  }
   const int tpc = e->mode == SPKGPU_ENSEMBLE_LAUNCHES4 ? 4 : (e->mode == SPKGPU_ENSEMBLE_LAUNCHES2 ? 2 : 1);
   const unsigned grid = (unsigned)((e->ntiles + tpc - 1) / tpc);
   if (e->d.app == SPKGPU_ISING) {
@@ -609,14 +652,21 @@ static cudaError_t ens_reset(spkgpu_ensemble *e) {
 // Autotuner: times one captured step of each mode on this replica set
 // (after a warm-up step, sites all 1) and keeps the faster; the choice is
 // cached per (app, replicas, tiles, exchange period) for the process.
-// SPKGPU_ENSEMBLE_MODE=persistent|launches forces a mode.
-static const char *const kModeNames[SPKGPU_ENSEMBLE_NMODES] = {"persistent", "launches", "launches2", "launches4"};
+// SPKGPU_ENSEMBLE_MODE=persistent|launches|launches2|launches4|warps forces a
+// mode (warps only for Ising).
+static const char *const kModeNames[SPKGPU_ENSEMBLE_NMODES] = {"persistent", "launches", "launches2", "launches4",
+                                                                "warps"};
+
+// the warp form sweeps Ising sites only
+static bool ens_mode_ok(const spkgpu_ensemble *e, int mode) {
+  return mode != SPKGPU_ENSEMBLE_WARPS || e->d.app == SPKGPU_ISING;
+}
 
 static int ens_pick_mode(spkgpu_ensemble *e, float *ms_out) {
   for (int m = 0; m < SPKGPU_ENSEMBLE_NMODES; m++) ms_out[m] = -1.0f;
   if (const char *env = getenv("SPKGPU_ENSEMBLE_MODE")) {
     for (int m = 0; m < SPKGPU_ENSEMBLE_NMODES; m++)
-      if (!strcmp(env, kModeNames[m])) return m;
+      if (!strcmp(env, kModeNames[m]) && ens_mode_ok(e, m)) return m;
   }
   static std::mutex mu;
   static std::map<std::vector<int64_t>, int> cache;
@@ -629,6 +679,7 @@ static int ens_pick_mode(spkgpu_ensemble *e, float *ms_out) {
   int best = SPKGPU_ENSEMBLE_PERSISTENT;
   float best_ms = -1.0f;
   for (int mode = 0; mode < SPKGPU_ENSEMBLE_NMODES; mode++) {
+    if (!ens_mode_ok(e, mode)) continue;
     e->mode = mode;
     ens_capture(e);
     if (!e->gexec) continue;
@@ -669,6 +720,8 @@ int spkgpu_ensemble_destroy(spkgpu_ensemble *e) {
   cudaFree(e->d_tile_start);
   cudaFree(e->d_tile_rep);
   cudaFree(e->d_tile_pos);
+  cudaFree(e->d_pair_rep);
+  cudaFree(e->d_pair_tile);
   cudaFree(e->d_nacc_slots);
   cudaFree(e->d_tidx);
   cudaFree(e->d_group_start);
@@ -739,6 +792,15 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
       tile_pos[t] = make_int2(r, ((lt / tpr) << 16) | (lt % tpr));
     }
   }
+  // warp form: consecutive tiles of a replica in pairs (an odd last tile alone)
+  std::vector<int32_t> pair_rep, pair_tile;
+  for (int r = 0; r < n; r++)
+    for (int t = tile_start[r]; t < tile_start[r + 1]; t += 2) {
+      pair_rep.push_back(r);
+      pair_tile.push_back(t);
+      pair_tile.push_back(t + 1 < tile_start[r + 1] ? t + 1 : -1);
+    }
+  e->npairs = (int)pair_rep.size();
   // temperatures: index t = the replica that started with it
   std::vector<uint64_t> thr((size_t)n * 5);
   std::vector<double> beta(n);
@@ -785,8 +847,12 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
       !dmalloc((void **)&e->d_last_bonds, n * 8) || !dmalloc((void **)&e->d_ctl, sizeof(EnsCtl)) ||
       !dmalloc((void **)&e->d_bad, sizeof(int)) || !dmalloc((void **)&e->d_tile_rep, (size_t)e->ntiles * 4) ||
       !dmalloc((void **)&e->d_nacc_slots, kCounterSlots * sizeof(unsigned long long)) ||
-      !dmalloc((void **)&e->d_slot_group, n * 4) || !dmalloc((void **)&e->d_tile_pos, (size_t)e->ntiles * 8))
+      !dmalloc((void **)&e->d_slot_group, n * 4) || !dmalloc((void **)&e->d_tile_pos, (size_t)e->ntiles * 8) ||
+      !dmalloc((void **)&e->d_pair_rep, (size_t)e->npairs * 4) ||
+      !dmalloc((void **)&e->d_pair_tile, (size_t)e->npairs * 8))
     return fail(SPKGPU_ERR_NOMEM);
+  cudaMemcpy(e->d_pair_rep, pair_rep.data(), (size_t)e->npairs * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(e->d_pair_tile, pair_tile.data(), (size_t)e->npairs * 8, cudaMemcpyHostToDevice);
   cudaMemcpy(e->d_tile_pos, tile_pos.data(), (size_t)e->ntiles * 8, cudaMemcpyHostToDevice);
   cudaMemcpy(e->d_slot_group, slot_group.data(), n * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(e->d_tile_rep, tile_rep.data(), (size_t)e->ntiles * 4, cudaMemcpyHostToDevice);
@@ -839,6 +905,9 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   a.seed = d.seed;
   a.ctl = e->d_ctl;
   a.nacc_slots = e->d_nacc_slots;
+  a.pair_rep = e->d_pair_rep;
+  a.pair_tile = e->d_pair_tile;
+  a.npairs = e->npairs;
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
   // pick the faster execution form for this replica set, then start from a
   // clean state and capture one step of it as a graph

@@ -2,11 +2,14 @@
 // 32x32 tile, both colours of the sweep in shared memory (tile_sweep.cuh),
 // reading one buffer and writing the other.  Used by spkgpu_sweep for sq/4n
 // lattices without sectors, mask or strict RNG whose extents are multiples of
-// 32; every other configuration takes the generic phase kernel.
+// 32; every other configuration takes the generic phase kernel.  Ising on
+// int8 buffers with 16-byte alignment takes the warp form (warp_tile.cuh):
+// one tile per warp, two per CTA, same draws and results.
 
 #include "counters.cuh"
 #include "spk_internal.h"
 #include "tile_sweep.cuh"
+#include "warp_tile.cuh"
 
 namespace spk {
 
@@ -42,6 +45,32 @@ __global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
               (unsigned long long)w);
 }
 
+__global__ void __launch_bounds__(64, 32) fused2d_warp_kernel(FusedArgs a) {
+  __shared__ __align__(16) int8_t stage[2][kWStageBytes];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tpr = a.nx / kTile;
+  const int t = 2 * blockIdx.x + warp;
+  if (t >= tpr * (a.ny / kTile)) return;
+  TileJob j;
+  j.src = a.src;
+  j.dst = a.dst;
+  j.L = a.nx;
+  j.Ly = a.ny;
+  j.x0 = (t % tpr) * kTile;
+  j.y0 = (t / tpr) * kTile;
+  j.base = 0;
+  j.seed = a.seed;
+  j.key1 = kStreamSweep;
+  j.sweep = a.sweep;
+  j.nspins = a.nspins;
+  j.replica = 0;
+  j.thr = nullptr;
+  j.t2 = a.acc.thr[2];
+  j.t4 = a.acc.thr[4];
+  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8(j, stage[warp], lane));
+  if (lane == 0 && w) atomicAdd(&a.naccept[t & (kCounterSlots - 1)], (unsigned long long)w);
+}
+
 bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny) {
   (void)app;
   return lattice == SPKGPU_SQ_4N && nx % kTile == 0 && ny % kTile == 0 &&
@@ -51,6 +80,12 @@ bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny) {
 template <typename S>
 static cudaError_t launch_fused_t(int app, const FusedArgs &a, cudaStream_t s) {
   unsigned tiles = (unsigned)((a.nx / kTile) * (a.ny / kTile));
+  if constexpr (sizeof(S) == 1) {
+    if (app == SPKGPU_ISING && ((uintptr_t)a.src | (uintptr_t)a.dst) % 16 == 0) {
+      fused2d_warp_kernel<<<(tiles + 1) / 2, 64, 0, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
   switch (app) {
     case SPKGPU_ISING: fused2d_kernel<SPKGPU_ISING, S><<<tiles, kTileThreads, 0, s>>>(a); break;
     case SPKGPU_POTTS: fused2d_kernel<SPKGPU_POTTS, S><<<tiles, kTileThreads, 0, s>>>(a); break;

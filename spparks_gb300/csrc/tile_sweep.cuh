@@ -54,6 +54,7 @@ struct TileJob {
   int nspins;
   int replica;        // ensemble: temperature index of the tile's replica
   const uint64_t *thr;  // thr[dE], dE = 0..4 (all 0 at zero temperature)
+  uint64_t t2, t4;      // thr[2] and thr[4] in registers (warp_tile.cuh)
 };
 
 __device__ __forceinline__ int stage_at(int lx, int ly) { return (ly + kHalo) * kStageX + lx + kXOff; }

@@ -1,0 +1,239 @@
+// One whole sq/4n colour sweep of a 32x32 tile of Ising sites stored as int8,
+// swept by ONE warp (AppIsing::site_event_rejection, src/app_ising.cpp:104-136,
+// under AppLattice::iterate_rejection with sweep color,
+// src/app_lattice.cpp:672-680: colour 1, then colour 2).
+//
+// Same schedule and draws as tile_sweep.cuh (stage with a two-row halo,
+// colour-1 sites of the tile and of its one-site ring first, then the
+// colour-2 sites), with three differences that cut the work per site:
+//   * one warp owns the tile, so the two phases are separated by __syncwarp,
+//     and a CTA of two warps sweeps two tiles of one lattice (one Philox key);
+//   * the Philox blocks and lane codes are computed while the tile's staging
+//     copies are in flight (they do not depend on site values);
+//   * the stage holds 16 halo columns on each side so that every row is four
+//     16-byte cp.async chunks.
+//
+// Lane arithmetic.  Each 32-bit word holds four sites (byte lanes), values 1
+// or 2.  For a lane with value v and neighbour values summing to S (4..8):
+//   unlike neighbours e = S - 4 (v = 1) or 8 - S (v = 2) = (S ^ X) - 3v - 1,
+//   with X = 15 where v = 2 and 0 where v = 1 (15 - S = S ^ 15 for S <= 15).
+// The draws of a site are folded into one code byte
+//   0x9D + lvl - 0x40 p,  lvl = [x1 < thr[4]] + [x1 < thr[2]],  p = [x0 < 2^31-1]
+// (a threshold of 2^32 passes every draw: its test is counted in the start
+// value and the compare is made against 0),
+// so that s = (S ^ X) + code - 3v = e + lvl + 0x1E + 0x40 (2 - p) per lane:
+// bits 0-5 stay below 0x25, bit 5 is set iff e + lvl >= 2 (the flip, or a
+// proposal equal to the current value, is accepted: e >= 2 means dE <= 0;
+// e = 1 needs x1 < thr[2]; e = 0 needs x1 < thr[4], and thr[4] <= thr[2]),
+// and bits 6-7 hold the proposed value 2 - p.  The new lane value is the
+// proposal where bit 5 is set in a lane of the phase's colour, else v.  No
+// step carries or borrows across lanes.  At zero temperature thr[] is all
+// zero, so lvl = 0 and only e >= 2 is accepted.
+//
+// Site values must be 1 or 2 (uploads check the range).  The Philox site
+// counter of a tile is its lattice index (TileJob::base is not used): with
+// x0 and L multiples of 32, every 8-site segment starts at a multiple of 8.
+#pragma once
+
+#include <stdint.h>
+
+#include "spk_philox.cuh"
+#include "tile_sweep.cuh"
+
+namespace spk {
+
+constexpr int kWXOff = 16;                          // halo columns on each side
+constexpr int kWStageX = kTile + 2 * kWXOff;        // 64 bytes per staged row
+constexpr int kWStageBytes = kWStageX * kStageY;    // 2304
+constexpr int kWChunks = kStageY * kWStageX / 16;   // 144 chunks of 16 bytes
+constexpr int kWSegPerLane = kTile * kTile / 8 / 32;  // 4 segments of 8 sites
+static_assert(kWSegPerLane * 8 * 32 == kTile * kTile, "segments must cover the tile");
+static_assert(kRing == 2 * 32, "two ring sites per lane");
+
+__device__ __forceinline__ int wstage_at(int lx, int ly) { return (ly + kHalo) * kWStageX + lx + kWXOff; }
+
+// Issue the staging of the tile (rows y0-2 .. y0+33, columns x0-16 .. x0+47,
+// periodic wrap) as 16-byte cp.async copies; the caller commits, waits and
+// synchronises the warp.  src and L must keep every chunk 16-byte aligned.
+__device__ __forceinline__ void warp_stage_async(const TileJob &j, int8_t *stage, int lane) {
+  const int8_t *src = (const int8_t *)j.src;
+#pragma unroll
+  for (int m = 0; m < (kWChunks + 31) / 32; m++) {
+    const int k = lane + 32 * m;
+    if (k < kWChunks) {
+      const int ly = k >> 2, wc = k & 3;
+      int gy = j.y0 + ly - kHalo, gx = j.x0 - kWXOff + 16 * wc;
+      gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
+      gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
+      const void *g = src + (int64_t)gy * j.L + gx;
+      const unsigned sa = (unsigned)__cvta_generic_to_shared(stage + ly * kWStageX + 16 * wc);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
+    }
+  }
+}
+
+// c + INC if x < t (unsigned), as a compare and a predicated add of an
+// immediate (a constant in a register would stay live across the draws)
+template <uint32_t INC>
+__device__ __forceinline__ uint32_t add_if_below(uint32_t c, uint32_t x, uint32_t t) {
+  asm("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %1, %2;\n\t@q add.u32 %0, %0, %3;\n\t}"
+      : "+r"(c)
+      : "r"(x), "r"(t), "n"(INC));
+  return c;
+}
+
+// adds the code of a site with draws (x0, x1) to the byte at bit SH of c,
+// which starts at 0x9D plus the number of threshold tests that always pass
+// (thr >= 2^32); t2c and t4c are the thresholds below 2^32, else 0
+template <int SH>
+__device__ __forceinline__ uint32_t add_lane_code(uint32_t c, uint32_t x0, uint32_t x1, uint32_t t2c, uint32_t t4c) {
+  asm("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %1, 0x7FFFFFFF;\n\t@q add.u32 %0, %0, %2;\n\t}"
+      : "+r"(c)
+      : "r"(x0), "n"(0u - (0x40u << SH)));
+  c = add_if_below<1u << SH>(c, x1, t4c);
+  return add_if_below<1u << SH>(c, x1, t2c);
+}
+
+// ring site k (0..63) of the tile, as in ring_site: rows -1 and 32, then
+// columns -1 and 32, sixteen colour-1 sites each
+__device__ __forceinline__ void warp_ring_pos(int k, int &rlx, int &rly) {
+  const int q = k & (kTile / 2 - 1);
+  if (k < kTile / 2) {
+    rly = -1;
+    rlx = 2 * q + 1;
+  } else if (k < kTile) {
+    rly = kTile;
+    rlx = 2 * q;
+  } else if (k < 3 * kTile / 2) {
+    rlx = -1;
+    rly = 2 * q + 1;
+  } else {
+    rlx = kTile;
+    rly = 2 * q;
+  }
+}
+
+// the codes of a lane's sites: segment m (row (lane>>2) + 8m, columns
+// 8(lane&3) .. +7) in code[2m] (lanes 0-3) and code[2m+1] (lanes 4-7); the
+// lane's ring sites k = lane and lane+32 in the low bytes of ring[]
+struct WarpDraws {
+  uint32_t code[2 * kWSegPerLane];
+  uint32_t ring[2];
+};
+
+__device__ __forceinline__ void warp_draws(const TileJob &j, int lane, WarpDraws &d) {
+  const RoundKeys rk = round_keys(j.seed, j.key1);
+  const bool big2 = (j.t2 >> 32) != 0, big4 = (j.t4 >> 32) != 0;
+  const uint32_t t2c = big2 ? 0u : (uint32_t)j.t2, t4c = big4 ? 0u : (uint32_t)j.t4;
+  const uint32_t c0 = 0x9D9D9D9Du + 0x01010101u * ((big2 ? 1u : 0u) + (big4 ? 1u : 0u));
+  // the ring first: its codes then stay live in two registers only
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    int rlx, rly;
+    warp_ring_pos(lane + 32 * r, rlx, rly);
+    int gy = j.y0 + rly, gx = j.x0 + rlx;
+    gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
+    gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
+    const int64_t s = (int64_t)gy * j.L + gx;
+    const U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), j.sweep, 0u}, rk);
+    const bool odd = s & 1;
+    d.ring[r] = add_lane_code<0>(c0 & 0xFFu, odd ? w.z : w.x, odd ? w.w : w.y, t2c, t4c);
+  }
+#pragma unroll
+  for (int m = 0; m < kWSegPerLane; m++) {
+    const int ly = (lane >> 2) + 8 * m;
+    const int64_t s = (int64_t)(j.y0 + ly) * j.L + j.x0 + 8 * (lane & 3);
+    const uint32_t plo = (uint32_t)(s >> 1), phi = (uint32_t)(s >> 33);  // plo % 4 == 0
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const U4 w0 = philox4x32_10_rk(U4{plo + (uint32_t)(2 * h), phi, j.sweep, 0u}, rk);
+      uint32_t c = add_lane_code<0>(c0, w0.x, w0.y, t2c, t4c);
+      c = add_lane_code<8>(c, w0.z, w0.w, t2c, t4c);
+      const U4 w1 = philox4x32_10_rk(U4{plo + (uint32_t)(2 * h + 1), phi, j.sweep, 0u}, rk);
+      c = add_lane_code<16>(c, w1.x, w1.y, t2c, t4c);
+      d.code[2 * m + h] = add_lane_code<24>(c, w1.z, w1.w, t2c, t4c);
+    }
+  }
+}
+
+// new values of four lanes v with neighbour words l, u, dn, r and codes
+// `code`; cm = 0x20 in the lanes of the phase's colour
+__device__ __forceinline__ uint32_t warp_lanes(uint32_t v, uint32_t l, uint32_t u, uint32_t dn, uint32_t r,
+                                               uint32_t code, uint32_t cm) {
+  const uint32_t sum = l + u + dn + r;
+  const uint32_t x = v * 15u - 0x0F0F0F0Fu;
+  const uint32_t s = (sum ^ x) + (code - 3u * v);
+  const uint32_t am = (s & cm) * 6u;  // bits 6-7 of the accepted lanes
+  return ((s & am) | ((v << 6) & ~am)) >> 6;
+}
+
+// one colour phase of segment m: reads the stage, returns the new segment
+__device__ __forceinline__ uint2 warp_segment(const int8_t *stage, int c, const WarpDraws &d, int m, uint32_t cm,
+                                              uint2 &v) {
+  v = *(const uint2 *)(stage + c);
+  const uint2 up = *(const uint2 *)(stage + c - kWStageX);
+  const uint2 dn = *(const uint2 *)(stage + c + kWStageX);
+  const uint32_t lw = *(const uint32_t *)(stage + c - 4);  // top byte: site x0-1
+  const uint32_t rw = *(const uint32_t *)(stage + c + 8);  // low byte: site x0+8
+  uint2 n;
+  n.x = warp_lanes(v.x, __funnelshift_l(lw, v.x, 8), up.x, dn.x, __funnelshift_r(v.x, v.y, 8), d.code[2 * m], cm);
+  n.y = warp_lanes(v.y, __funnelshift_l(v.x, v.y, 8), up.y, dn.y, __funnelshift_r(v.y, rw, 8), d.code[2 * m + 1],
+                   cm);
+  return n;
+}
+
+// Both colour phases of the staged tile (warp_stage_async, waited for and
+// followed by __syncwarp); the tile's final values go to j.dst.  Returns the
+// number of this lane's sites that changed.
+__device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *stage, int lane, const WarpDraws &d) {
+  int8_t *dst = (int8_t *)j.dst;
+  const int x0 = 8 * (lane & 3);
+  // colour-1 lanes have the parity of the row; rows of a lane share a parity
+  const uint32_t cm1 = ((lane >> 2) & 1) ? 0x20002000u : 0x00200020u;
+  const uint32_t cm2 = cm1 ^ 0x20202020u;
+  uint32_t cnt = 0;  // 3 per changed site, per byte lane
+#pragma unroll
+  for (int m = 0; m < kWSegPerLane; m++) {
+    const int c = wstage_at(x0, (lane >> 2) + 8 * m);
+    uint2 v;
+    const uint2 n = warp_segment(stage, c, d, m, cm1, v);
+    cnt += (v.x ^ n.x) + (v.y ^ n.y);
+    *(uint2 *)(stage + c) = n;
+  }
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    int rlx, rly;
+    warp_ring_pos(lane + 32 * r, rlx, rly);
+    const int c = wstage_at(rlx, rly);
+    const uint32_t own = (uint8_t)stage[c];
+    const uint32_t sum =
+        (uint32_t)(uint8_t)stage[c - 1] + (uint8_t)stage[c + 1] + (uint8_t)stage[c - kWStageX] +
+        (uint8_t)stage[c + kWStageX];
+    const uint32_t s = (sum ^ (own * 15u - 15u)) + (d.ring[r] - 3u * own);
+    if ((s & 0x20u) && (s >> 6) != own) stage[c] = (int8_t)(s >> 6);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int m = 0; m < kWSegPerLane; m++) {
+    const int ly = (lane >> 2) + 8 * m;
+    uint2 v;
+    const uint2 n = warp_segment(stage, wstage_at(x0, ly), d, m, cm2, v);
+    cnt += (v.x ^ n.x) + (v.y ^ n.y);
+    *(uint2 *)(dst + (int64_t)(j.y0 + ly) * j.L + j.x0 + x0) = n;
+  }
+  return ((cnt * 0x01010101u) >> 24) / 3u;
+}
+
+// stage, draws, then both phases of one tile; j.t2 and j.t4 are the
+// thresholds thr[2] and thr[4] (thr[2] >= thr[4]); returns this lane's changes
+__device__ __forceinline__ unsigned int warp_tile_ising8(const TileJob &j, int8_t *stage, int lane) {
+  warp_stage_async(j, stage, lane);
+  cp_async_commit();
+  WarpDraws d;
+  warp_draws(j, lane, d);
+  cp_async_wait<0>();
+  __syncwarp();
+  return warp_phases(j, stage, lane, d);
+}
+
+}  // namespace spk

@@ -49,9 +49,10 @@ def ensemble_case(seed=777):
     return L, T, spins
 
 
-@pytest.fixture(params=["persistent", "launches", "launches2", "launches4"])
+@pytest.fixture(params=["persistent", "launches", "launches2", "launches4", "warps"])
 def mode(request, monkeypatch):
-    """both execution forms of the ensemble, forced past the autotuner"""
+    """every execution form of the ensemble, forced past the autotuner (the
+    warp form is Ising only: a Potts ensemble then takes the autotuner's)"""
     monkeypatch.setenv("SPKGPU_ENSEMBLE_MODE", request.param)
     return request.param
 
@@ -102,7 +103,7 @@ def test_autotuner_times_both_forms_then_caches(sg, monkeypatch):
     monkeypatch.delenv("SPKGPU_ENSEMBLE_MODE", raising=False)
     L, T = [64, 96, 32, 64, 32], [1.8, 2.2, 2.6, 3.0, 3.4]  # a replica set no other test uses
     first = sg.Ensemble(L, T, "ising", 2, seed=1, exchange_every=5).mode()
-    assert first["mode"] in ("persistent", "launches")
+    assert first["mode"] in sg.ENSEMBLE_MODES
     assert all(v is not None and v > 0 for v in first["tune_ms"].values())
     again = sg.Ensemble(L, T, "ising", 2, seed=2, exchange_every=5).mode()
     assert again["mode"] == first["mode"]

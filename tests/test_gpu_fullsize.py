@@ -61,14 +61,14 @@ def test_c1_neighonly_sc26n_256_int16_rows_equal_phase_kernel(sg):
 
 def test_c2_ensemble_512_replicas_both_forms_agree(sg, monkeypatch):
     """the full 512-replica ensemble: every execution form (persistent, one
-    launch per sweep with 1, 2 or 4 tiles per CTA) gives the same sites,
+    launch per sweep with 1, 2 or 4 tiles per CTA, one tile per warp) gives the same sites,
     temperatures, energies and counters after two exchange periods"""
     import bench
 
     L, T = bench.ensemble_config(seed=bench.SEED)
     spins = bench.init_spins(L, seed=bench.SEED)
     res = []
-    for mode in ("persistent", "launches", "launches2", "launches4"):
+    for mode in sg.ENSEMBLE_MODES:
         monkeypatch.setenv("SPKGPU_ENSEMBLE_MODE", mode)
         ens = sg.Ensemble(L, T, "ising", 2, seed=bench.SEED, exchange_every=10)
         ens.upload(spins)
