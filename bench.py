@@ -336,7 +336,8 @@ def run_ours(args):
     # dominant kernel: the persistent kernel (all sweeps of a step) or the
     # per-sweep launch; int8 sites, one read and one write per update
     persistent = ens_mode["mode"] == "persistent"
-    kname = "ensemble_kernel" if persistent else "ensemble_sweep_kernel"
+    kname = ("ensemble_kernel" if persistent else
+             "ensemble_warp_kernel" if ens_mode["mode"] == "warps" else "ensemble_sweep_kernel")
     alg_bytes = 2.0 * 1.0 * nsites * (SWEEPS_PER_STEP if persistent else 1)
     kernel_ms = kern_ms / max(kern_launches, 1)
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
