@@ -252,6 +252,17 @@ int spkgpu_ensemble_download(spkgpu_ensemble *e, int32_t *spin, int64_t n);
    captured CUDA graph of one step */
 int spkgpu_ensemble_run(spkgpu_ensemble *e, int32_t nsweeps);
 int spkgpu_ensemble_timed_run(spkgpu_ensemble *e, int32_t nsweeps, float *ms);
+/* Pipelined host I/O: enqueue one step that loads every site value from
+   `in` (host, int32, replicas in order), runs nsweeps sweeps and stores the
+   result into `out` (host, int32), and return at once.  With page-locked
+   buffers (cudaHostAlloc or cudaHostRegister) the copy engines move a call's
+   input while the previous call's sweeps run and its result while the next
+   call's sweeps run (two int32 device staging buffers of every site are
+   allocated on the first call).  Both buffers must stay untouched until
+   spkgpu_ensemble_synchronize returns; that call reports invalid input values
+   (SPKGPU_ERR_INVALID_SPIN), found after the sweeps have run on them.
+   Pageable buffers take upload, run and download in turn (synchronous). */
+int spkgpu_ensemble_run_io(spkgpu_ensemble *e, const int32_t *in, int32_t *out, int32_t nsweeps);
 int spkgpu_ensemble_synchronize(spkgpu_ensemble *e);
 int spkgpu_ensemble_get_stats(spkgpu_ensemble *e, spkgpu_ensemble_stats *out);
 /* current temperature of each replica and energy (unlike-neighbour bonds,

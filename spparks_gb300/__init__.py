@@ -104,6 +104,7 @@ EXPORTS = [
     "spkgpu_device_spins", "spkgpu_launch_count", "spkgpu_kmc_setup", "spkgpu_kmc_run", "spkgpu_kmc_run_until",
     "spkgpu_ensemble_create", "spkgpu_ensemble_destroy", "spkgpu_ensemble_last_error", "spkgpu_ensemble_upload",
     "spkgpu_ensemble_download", "spkgpu_ensemble_run", "spkgpu_ensemble_timed_run", "spkgpu_ensemble_synchronize",
+    "spkgpu_ensemble_run_io",
     "spkgpu_ensemble_get_stats", "spkgpu_ensemble_temperatures", "spkgpu_ensemble_energies",
     "spkgpu_ensemble_launch_count", "spkgpu_ensemble_mode", "spkgpu_ensemble_sweep_kernel_ms",
     "spkgpu_sweep_sq4_noalloc", "spkgpu_philox_rate",
@@ -158,6 +159,7 @@ def load_library(path: Path | None = None):
     L.spkgpu_ensemble_upload.argtypes = [vp, P(ctypes.c_int32), ctypes.c_int64]
     L.spkgpu_ensemble_download.argtypes = [vp, P(ctypes.c_int32), ctypes.c_int64]
     L.spkgpu_ensemble_run.argtypes = [vp, ctypes.c_int32]
+    L.spkgpu_ensemble_run_io.argtypes = [vp, P(ctypes.c_int32), P(ctypes.c_int32), ctypes.c_int32]
     L.spkgpu_ensemble_timed_run.argtypes = [vp, ctypes.c_int32, P(ctypes.c_float)]
     L.spkgpu_ensemble_synchronize.argtypes = [vp]
     L.spkgpu_ensemble_get_stats.argtypes = [vp, P(EnsembleStats)]
@@ -384,6 +386,16 @@ class Ensemble:
 
     def run(self, nsweeps):
         self._check(self.lib.spkgpu_ensemble_run(self.h, int(nsweeps)))
+
+    def run_io(self, spin_in: np.ndarray, spin_out: np.ndarray, nsweeps):
+        """Enqueue one step: load spin_in, run nsweeps sweeps, store into
+        spin_out (both int32, every site; page-locked memory makes
+        successive steps overlap).  Neither array may change until
+        synchronize() returns, which also reports invalid input values."""
+        for a in (spin_in, spin_out):
+            if a.dtype != np.int32 or not a.flags["C_CONTIGUOUS"] or a.size != self.nsites:
+                raise ValueError("run_io wants contiguous int32 arrays of every site")
+        self._check(self.lib.spkgpu_ensemble_run_io(self.h, _i32p(spin_in), _i32p(spin_out), int(nsweeps)))
 
     def timed_run(self, nsweeps) -> float:
         ms = ctypes.c_float()

@@ -498,6 +498,12 @@ struct spkgpu_ensemble {
   float tune_ms[SPKGPU_ENSEMBLE_NMODES] = {-1.0f, -1.0f, -1.0f, -1.0f, -1.0f};  // the autotuner's step times per mode
   int32_t *d_pair_rep = nullptr, *d_pair_tile = nullptr;
   int npairs = 0;
+  // pipelined host I/O (spkgpu_ensemble_run_io): int32 device staging of
+  // the input and the output, one copy stream per direction, events between
+  int32_t *io_in32 = nullptr, *io_out32 = nullptr;
+  cudaStream_t io_in = nullptr, io_out = nullptr;
+  cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_snap_ready = nullptr, ev_snap_free = nullptr;
+  bool io_pending = false;  // run_io calls since the last synchronize (bad-value flag armed)
   int64_t enq = 0;  // sweeps enqueued so far (the host's copy of ctl->sweep)
   std::vector<int32_t> slot_init;  // replica in each exchange slot at creation
   int64_t *d_base = nullptr;
@@ -712,6 +718,8 @@ const char *spkgpu_ensemble_last_error(const spkgpu_ensemble *e) { return e ? e-
 int spkgpu_ensemble_destroy(spkgpu_ensemble *e) {
   if (!e) return SPKGPU_ERR_ARG;
   if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->io_in) cudaStreamSynchronize(e->io_in);
+  if (e->io_out) cudaStreamSynchronize(e->io_out);
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
   if (e->graph) cudaGraphDestroy(e->graph);
   cudaFree(e->buf[0]);
@@ -740,6 +748,12 @@ int spkgpu_ensemble_destroy(spkgpu_ensemble *e) {
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->kev0) cudaEventDestroy(e->kev0);
   if (e->kev1) cudaEventDestroy(e->kev1);
+  cudaFree(e->io_in32);
+  cudaFree(e->io_out32);
+  for (cudaEvent_t ev : {e->ev_in_ready, e->ev_in_free, e->ev_snap_ready, e->ev_snap_free})
+    if (ev) cudaEventDestroy(ev);
+  if (e->io_in) cudaStreamDestroy(e->io_in);
+  if (e->io_out) cudaStreamDestroy(e->io_out);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return SPKGPU_OK;
@@ -1022,9 +1036,75 @@ int spkgpu_ensemble_timed_run(spkgpu_ensemble *e, int32_t nsweeps, float *ms) {
   return SPKGPU_OK;
 }
 
+// Pipelined host I/O.  Per call, on three streams:
+//   io_in:   (once the previous call's input was converted) DMA of the input,
+//            page-locked host int32 -> io_in32
+//   stream:  io_in32 -> current buffer (int8, checked), the sweeps, current
+//            buffer -> io_out32 (once the previous call's output left)
+//   io_out:  DMA of io_out32 -> page-locked host int32
+// The copy engines move one call's input and the previous call's output
+// while the SMs sweep: kernels that read or write host memory directly would
+// hold SMs for the whole transfer and serialise with the sweeps.
+static int ens_io_setup(spkgpu_ensemble *e) {
+  if (e->io_in) return SPKGPU_OK;
+  const size_t bytes = (size_t)e->nsites * sizeof(int32_t);
+  if (cudaMalloc((void **)&e->io_in32, bytes) != cudaSuccess || cudaMalloc((void **)&e->io_out32, bytes) != cudaSuccess)
+    return ens_fail(e, SPKGPU_ERR_NOMEM, "run_io staging buffers");
+  for (cudaEvent_t *ev : {&e->ev_in_ready, &e->ev_in_free, &e->ev_snap_ready, &e->ev_snap_free})
+    ENS_CUDA(e, cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  ENS_CUDA(e, cudaStreamCreateWithFlags(&e->io_in, cudaStreamNonBlocking));
+  ENS_CUDA(e, cudaStreamCreateWithFlags(&e->io_out, cudaStreamNonBlocking));
+  ENS_CUDA(e, cudaEventRecord(e->ev_in_free, e->stream));
+  ENS_CUDA(e, cudaEventRecord(e->ev_snap_free, e->stream));
+  return SPKGPU_OK;
+}
+
+int spkgpu_ensemble_run_io(spkgpu_ensemble *e, const int32_t *in, int32_t *out, int32_t nsweeps) {
+  if (!e || !in || !out || nsweeps < 0) return SPKGPU_ERR_ARG;
+  if (!mapped_host_ptr(in) || !mapped_host_ptr(out)) {  // pageable: the three steps in turn
+    int rc = spkgpu_ensemble_upload(e, in, e->nsites);
+    if (!rc) rc = ens_enqueue(e, nsweeps);
+    if (!rc) rc = spkgpu_ensemble_download(e, out, e->nsites);
+    return rc;
+  }
+  int rc = ens_io_setup(e);
+  if (rc) return rc;
+  const int64_t n = e->nsites;
+  const size_t bytes = (size_t)n * sizeof(int32_t);
+  if (!e->io_pending) {
+    ENS_CUDA(e, cudaMemsetAsync(e->d_bad, 0, sizeof(int), e->stream));
+    e->io_pending = true;
+  }
+  ENS_CUDA(e, cudaStreamWaitEvent(e->io_in, e->ev_in_free, 0));
+  ENS_CUDA(e, cudaMemcpyAsync(e->io_in32, in, bytes, cudaMemcpyHostToDevice, e->io_in));
+  ENS_CUDA(e, cudaEventRecord(e->ev_in_ready, e->io_in));
+  ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->ev_in_ready, 0));
+  ENS_CUDA(e, launch_convert_in(e->spin_bytes, e->io_in32, e->buf[e->parity], n, e->d.nspins, e->d_bad, e->stream));
+  ENS_CUDA(e, cudaEventRecord(e->ev_in_free, e->stream));
+  e->launches += 1;
+  rc = ens_enqueue(e, nsweeps);
+  if (rc) return rc;
+  ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->ev_snap_free, 0));
+  ENS_CUDA(e, launch_convert_out(e->spin_bytes, e->buf[e->parity], e->io_out32, n, e->stream));
+  ENS_CUDA(e, cudaEventRecord(e->ev_snap_ready, e->stream));
+  e->launches += 1;
+  ENS_CUDA(e, cudaStreamWaitEvent(e->io_out, e->ev_snap_ready, 0));
+  ENS_CUDA(e, cudaMemcpyAsync(out, e->io_out32, bytes, cudaMemcpyDeviceToHost, e->io_out));
+  ENS_CUDA(e, cudaEventRecord(e->ev_snap_free, e->io_out));
+  return SPKGPU_OK;
+}
+
 int spkgpu_ensemble_synchronize(spkgpu_ensemble *e) {
   if (!e) return SPKGPU_ERR_ARG;
   ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  if (e->io_in) ENS_CUDA(e, cudaStreamSynchronize(e->io_in));
+  if (e->io_out) ENS_CUDA(e, cudaStreamSynchronize(e->io_out));
+  if (e->io_pending) {
+    e->io_pending = false;
+    int bad = 0;
+    ENS_CUDA(e, cudaMemcpy(&bad, e->d_bad, sizeof(int), cudaMemcpyDeviceToHost));
+    if (bad) return ens_fail(e, SPKGPU_ERR_INVALID_SPIN, "One or more sites of a run_io input have invalid values");
+  }
   EnsCtl c;
   ENS_CUDA(e, cudaMemcpy(&c, e->d_ctl, sizeof(c), cudaMemcpyDeviceToHost));
   if (c.err) return ens_fail(e, SPKGPU_ERR_DEVICE, "grid barrier wait gave up");

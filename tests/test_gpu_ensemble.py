@@ -115,3 +115,54 @@ def test_ensemble_rejects_bad_sizes(sg):
         sg.Ensemble([48], [2.0])
     with pytest.raises(sg.SpkGpuError):
         sg.Ensemble([32], [0.0])
+
+
+def test_run_io_pipeline_equals_sequential_steps(sg):
+    """spkgpu_ensemble_run_io with page-locked buffers: three overlapping
+    steps, each from its own input, give the outputs, counters and
+    temperatures of upload / run / download in turn; pageable buffers take
+    the sequential path with the same results"""
+    import torch
+
+    L, T = [64, 32, 96, 64], [1.9, 2.3, 2.7, 3.1]
+    n = sum(l * l for l in L)
+    inputs = [oracle.init_spins(40 + k, n, 1, 2) for k in range(3)]
+    seq = sg.Ensemble(L, T, "ising", 2, seed=8, exchange_every=3)
+    want = []
+    for x in inputs:
+        seq.upload(x)
+        seq.run(6)
+        want.append(seq.download().tolist())
+    want_state = (seq.stats(), seq.temperatures().tolist())
+    seq.close()
+    for pinned in (True, False):
+        ens = sg.Ensemble(L, T, "ising", 2, seed=8, exchange_every=3)
+        if pinned:
+            ins = [torch.from_numpy(x.copy()).pin_memory().numpy() for x in inputs]
+            outs = [torch.zeros(n, dtype=torch.int32).pin_memory().numpy() for _ in inputs]
+        else:
+            ins = [x.copy() for x in inputs]
+            outs = [np.zeros(n, dtype=np.int32) for _ in inputs]
+        for x, y in zip(ins, outs):
+            ens.run_io(x, y, 6)
+        ens.synchronize()
+        assert [y.tolist() for y in outs] == want
+        assert (ens.stats(), ens.temperatures().tolist()) == want_state
+        ens.close()
+
+
+def test_run_io_reports_invalid_input_at_synchronize(sg):
+    import torch
+
+    L, T = [32, 64], [2.0, 2.5]
+    n = sum(l * l for l in L)
+    x = torch.from_numpy(oracle.init_spins(5, n, 1, 2)).pin_memory()
+    x[17] = 3
+    y = torch.zeros(n, dtype=torch.int32).pin_memory()
+    ens = sg.Ensemble(L, T, "ising", 2, seed=8, exchange_every=0)
+    ens.run_io(x.numpy(), y.numpy(), 2)
+    with pytest.raises(sg.SpkGpuError) as ei:
+        ens.synchronize()
+    assert ei.value.code == -6  # SPKGPU_ERR_INVALID_SPIN
+    ens.synchronize()  # the flag is cleared once reported
+    ens.close()
