@@ -21,7 +21,7 @@ def sg():
 @pytest.mark.parametrize("app,q,T", [("ising", 2, 2.269), ("potts", 20, 0.7), ("potts/neighonly", 9, 0.4),
                                      ("potts/neigh", 5, 1.1), ("ising", 2, 0.0), ("ising", 2, 1e30),
                                      ("potts", 7, 0.0), ("potts/neighonly", 5, 0.0)])
-@pytest.mark.parametrize("nx,ny,sb", [(64, 64, 1), (96, 32, 2), (32, 64, 4)])
+@pytest.mark.parametrize("nx,ny,sb", [(64, 64, 1), (96, 96, 1), (96, 32, 2), (32, 64, 4)])
 def test_fused_tile_sweep_matches_oracle(sg, app, q, T, nx, ny, sb):
     seed = 8642
     spin = oracle.init_spins(seed, nx * ny, 1, q)
