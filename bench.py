@@ -363,9 +363,9 @@ def run_ours(args):
         import oracle
 
         oracle.build()
-        r1, u1, w1 = cpu_rate(sample_replicas=48, sweeps=10, procs=1)
+        r1, u1, w1 = cpu_rate(sample_replicas=48, sweeps=40, procs=1)  # about 10 s of one core
         cpu = {"value": r1, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"48 random replicas x 10 sweeps ({u1:.3g} site-updates, {w1:.1f} s), oracle C "
+               "sample": f"48 random replicas x 40 sweeps ({u1:.3g} site-updates, {w1:.1f} s), oracle C "
                          "restatement of the reference colour sweep, 1 thread"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
