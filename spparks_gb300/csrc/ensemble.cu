@@ -417,8 +417,15 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) e
 
 // Ising, warp form: CTA b sweeps the tiles pair_tile[2b] and pair_tile[2b+1]
 // of replica pair_rep[b], one per warp (warp_tile.cuh); no block barrier.
+// Every launch lets the next sweep launch early (griddepcontrol); a sweep
+// launched as a programmatic dependent (AFTER_GRID: sweeps 2.. of a group,
+// which follow a sweep kernel, never the exchange) computes its draws while
+// the previous sweep finishes: the temperature index, thresholds and ctl it
+// reads before the wait are written only by the exchange launch.
+template <bool AFTER_GRID>
 __global__ void __launch_bounds__(64, 32) ensemble_warp_kernel(EnsArgs a, int k) {
   __shared__ __align__(16) int8_t stage[2][kWStageBytes];
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int t = a.pair_tile[2 * blockIdx.x + warp];
   if (t < 0) return;
@@ -443,7 +450,7 @@ __global__ void __launch_bounds__(64, 32) ensemble_warp_kernel(EnsArgs a, int k)
   j.thr = a.thr + (int64_t)j.replica * 5;
   j.t2 = j.thr[2];
   j.t4 = j.thr[4];
-  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8(j, stage[warp], lane));
+  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8<AFTER_GRID>(j, stage[warp], lane));
   if (lane == 0 && w)
     atomicAdd(&a.nacc_slots[(2 * blockIdx.x + warp) & (kCounterSlots - 1)], (unsigned long long)w);
 }
@@ -554,7 +561,20 @@ static cudaError_t ens_launch(spkgpu_ensemble *e, int nsweeps) {
 // one sweep launch of the per-sweep forms (1, 2 or 4 tiles per CTA)
 static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cudaStream_t st) {
   if (e->mode == SPKGPU_ENSEMBLE_WARPS) {
-    ensemble_warp_kernel<<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
+    if (k == 0) {
+      ensemble_warp_kernel<false><<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
+      return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)a.npairs);
+    cfg.blockDim = dim3(64);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, ensemble_warp_kernel<true>, a, k);
     return;
   }
   const int tpc = e->mode == SPKGPU_ENSEMBLE_LAUNCHES4 ? 4 : (e->mode == SPKGPU_ENSEMBLE_LAUNCHES2 ? 2 : 1);

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(64, 32) fused2d_warp_kernel(FusedArgs a) {
   j.thr = nullptr;
   j.t2 = a.acc.thr[2];
   j.t4 = a.acc.thr[4];
-  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8(j, stage[warp], lane));
+  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8<false>(j, stage[warp], lane));
   if (lane == 0 && w) atomicAdd(&a.naccept[t & (kCounterSlots - 1)], (unsigned long long)w);
 }
 

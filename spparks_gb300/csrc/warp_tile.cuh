@@ -56,19 +56,17 @@ __device__ __forceinline__ int wstage_at(int lx, int ly) { return (ly + kHalo) *
 // periodic wrap) as 16-byte cp.async copies; the caller commits, waits and
 // synchronises the warp.  src and L must keep every chunk 16-byte aligned.
 __device__ __forceinline__ void warp_stage_async(const TileJob &j, int8_t *stage, int lane) {
-  const int8_t *src = (const int8_t *)j.src;
-#pragma unroll
-  for (int m = 0; m < (kWChunks + 31) / 32; m++) {
-    const int k = lane + 32 * m;
-    if (k < kWChunks) {
-      const int ly = k >> 2, wc = k & 3;
-      int gy = j.y0 + ly - kHalo, gx = j.x0 - kWXOff + 16 * wc;
-      gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
-      gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
-      const void *g = src + (int64_t)gy * j.L + gx;
-      const unsigned sa = (unsigned)__cvta_generic_to_shared(stage + ly * kWStageX + 16 * wc);
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
-    }
+  // lane: chunk column lane & 3, rows (lane >> 2) + 8m; one chunk at a time
+  // (a rolled loop keeps a single address live)
+  int gx = j.x0 - kWXOff + 16 * (lane & 3);
+  gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
+  const int8_t *src = (const int8_t *)j.src + gx;
+  unsigned sa = (unsigned)__cvta_generic_to_shared(stage + (lane >> 2) * kWStageX + 16 * (lane & 3));
+#pragma unroll 1
+  for (int ly = lane >> 2; ly < kStageY; ly += 8, sa += 8 * kWStageX) {
+    int gy = j.y0 + ly - kHalo;
+    gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + (int64_t)gy * j.L) : "memory");
   }
 }
 
@@ -226,11 +224,23 @@ __device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *st
 
 // stage, draws, then both phases of one tile; j.t2 and j.t4 are the
 // thresholds thr[2] and thr[4] (thr[2] >= thr[4]); returns this lane's changes
+// AFTER_GRID: the kernel was launched as a programmatic dependent of the
+// previous sweep, whose output this tile reads: the draws (which read no
+// site) run first, then griddepcontrol.wait holds the warp until that grid
+// has completed and its writes are visible, then the tile is staged.
+template <bool AFTER_GRID>
 __device__ __forceinline__ unsigned int warp_tile_ising8(const TileJob &j, int8_t *stage, int lane) {
-  warp_stage_async(j, stage, lane);
-  cp_async_commit();
   WarpDraws d;
-  warp_draws(j, lane, d);
+  if (AFTER_GRID) {
+    warp_draws(j, lane, d);
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    warp_stage_async(j, stage, lane);
+    cp_async_commit();
+  } else {
+    warp_stage_async(j, stage, lane);
+    cp_async_commit();
+    warp_draws(j, lane, d);
+  }
   cp_async_wait<0>();
   __syncwarp();
   return warp_phases(j, stage, lane, d);
