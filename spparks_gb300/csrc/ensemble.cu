@@ -455,12 +455,50 @@ __global__ void __launch_bounds__(64, 32) ensemble_warp_kernel(EnsArgs a, int k)
     atomicAdd(&a.nacc_slots[(2 * blockIdx.x + warp) & (kCounterSlots - 1)], (unsigned long long)w);
 }
 
-// unlike bonds of every replica in the buffer the sweep k-1 wrote
-template <typename S>
-__global__ void __launch_bounds__(kTileThreads) ensemble_bonds_kernel(EnsArgs a, int k) {
+// unlike bonds (right and down neighbour of each site) of every replica in
+// the buffer the sweep k-1 wrote: one warp per 32x32 tile, lane = tile row,
+// read as two 16-byte loads; the row below comes from the next lane, the last
+// lane loads row 32 itself.  Eight int8 sites per 64-bit word, as in
+// tile_bonds.
+constexpr int kBondWarps = 8;
+
+__global__ void __launch_bounds__(32 * kBondWarps) ensemble_bonds_kernel(EnsArgs a, int k) {
+  const int t = blockIdx.x * kBondWarps + (threadIdx.x >> 5);
+  if (t >= a.ntiles) return;
+  const int lane = threadIdx.x & 31;
   const int parity = *(volatile int *)&a.ctl->parity ^ (k & 1);
-  const int t = blockIdx.x;
-  tile_bonds<S>(a, t, a.tile_rep[t], (const S *)(parity ? a.buf1 : a.buf0));
+  const int2 tp = a.tile_pos[t];
+  const int r = tp.x;
+  const int L = a.L[r];
+  const int x0 = (tp.y & 0xFFFF) * kTile, y0 = (tp.y >> 16) * kTile;
+  const uint8_t *rep = (const uint8_t *)(parity ? a.buf1 : a.buf0) + a.base[r];
+  const int y = y0 + lane;
+  const int xr = x0 + kTile == L ? 0 : x0 + kTile;
+  const uint4 *row = (const uint4 *)(rep + (int64_t)y * L + x0);
+  const uint4 p = row[0], q = row[1];
+  uint64_t w[4] = {(uint64_t)p.y << 32 | p.x, (uint64_t)p.w << 32 | p.z, (uint64_t)q.y << 32 | q.x,
+                   (uint64_t)q.w << 32 | q.z};
+  uint64_t dn[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) dn[i] = __shfl_down_sync(0xFFFFFFFFu, w[i], 1);
+  if (lane == 31) {
+    const int yd = y0 + kTile == L ? 0 : y0 + kTile;
+    const uint4 *below = (const uint4 *)(rep + (int64_t)yd * L + x0);
+    const uint4 bp = below[0], bq = below[1];
+    dn[0] = (uint64_t)bp.y << 32 | bp.x;
+    dn[1] = (uint64_t)bp.w << 32 | bp.z;
+    dn[2] = (uint64_t)bq.y << 32 | bq.x;
+    dn[3] = (uint64_t)bq.w << 32 | bq.z;
+  }
+  const uint64_t rb = rep[(int64_t)y * L + xr];
+  unsigned int b = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint64_t right = (w[i] >> 8) | ((i < 3 ? w[i + 1] : rb) << 56);
+    b += __popcll(lanes_nonzero(w[i] ^ right)) + __popcll(lanes_nonzero(w[i] ^ dn[i]));
+  }
+  const unsigned int s = __reduce_add_sync(0xFFFFFFFFu, b);
+  if (lane == 0 && s) atomicAdd(&a.bonds[r], (unsigned long long)s);
 }
 
 // one block: the exchange round (if `exchange`), then ctl moves on by m sweeps
@@ -596,7 +634,7 @@ static cudaError_t ens_launch_group(spkgpu_ensemble *e, int m, bool exchange, in
   const EnsArgs &a = e->args;
   const unsigned nt = (unsigned)e->ntiles;
   for (int k = 0; k < m; k++) launch_sweep(e, a, k, e->stream);
-  if (exchange) ensemble_bonds_kernel<int8_t><<<nt, kTileThreads, 0, e->stream>>>(a, m);
+  if (exchange) ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, e->stream>>>(a, m);
   ensemble_advance_kernel<<<1, 256, 0, e->stream>>>(a, m, exchange ? 1 : 0);
   *nk += m + (exchange ? 1 : 0) + 1;
   return cudaGetLastError();
@@ -634,7 +672,7 @@ static void ens_capture(spkgpu_ensemble *e) {
     for (int k = 0; k < e->chunk; k++) launch_sweep(e, a, k, cap);
     kev = kev && cudaEventRecordWithFlags(e->kev1, cap, cudaEventRecordExternal) == cudaSuccess;
     const bool exchange = e->d.exchange_every > 0;
-    if (exchange) ensemble_bonds_kernel<int8_t><<<nt, kTileThreads, 0, cap>>>(a, e->chunk);
+    if (exchange) ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, cap>>>(a, e->chunk);
     ensemble_advance_kernel<<<1, 256, 0, cap>>>(a, e->chunk, exchange ? 1 : 0);
     le = cudaGetLastError();
     (void)nk;
