@@ -9,7 +9,8 @@
 //                        each of its 32 x-pairs once and stores, for all 64
 //                        sites, four decision masks: the proposal (draw 0 >=
 //                        2^31-1 proposes value 2) and "draw 1 < thr[dE]" for
-//                        the three uphill moves dE = 2, 4, 6.
+//                        the three uphill moves dE = 2, 4, 6; each bit is a
+//                        32-bit compare and a predicated OR.
 //   packed_phase_kernel  per colour, one thread per word: the unlike count of
 //                        every site against its six neighbours as a
 //                        bit-sliced 3-bit sum of XOR masks; a site of the
@@ -32,26 +33,71 @@ struct PackedDecisions {
   uint64_t prop, a2, a4, a6;
 };
 
-__global__ void packed_draw_kernel(const PackedArgs a) {
-  int64_t nw = a.nwords;
-  int64_t words_per_row = a.nx >> 6;
+// c | BIT if x >= 2^31-1 (draw 0 proposes value 2), as a compare and a
+// predicated OR of an immediate
+template <uint32_t BIT>
+__device__ __forceinline__ uint32_t or_if_prop2(uint32_t c, uint32_t x) {
+  asm("{\n\t.reg .pred q;\n\tsetp.ge.u32 q, %1, 0x7FFFFFFF;\n\t@q or.b32 %0, %0, %2;\n\t}"
+      : "+r"(c)
+      : "r"(x), "n"(BIT));
+  return c;
+}
+
+// c | BIT if x < t
+template <uint32_t BIT>
+__device__ __forceinline__ uint32_t or_if_below(uint32_t c, uint32_t x, uint32_t t) {
+  asm("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %1, %2;\n\t@q or.b32 %0, %0, %3;\n\t}"
+      : "+r"(c)
+      : "r"(x), "r"(t), "n"(BIT));
+  return c;
+}
+
+// the four decision masks of a word, as 32-bit halves (index 0: bits 0-31)
+struct PackedHalves {
+  uint32_t prop[2], a2[2], a4[2], a6[2];
+};
+
+// x-pair M (sites 2M, 2M+1 of the word) and the pairs after it; the pair
+// index is a template argument so that every mask bit is an immediate
+template <int M>
+__device__ __forceinline__ void packed_pairs(uint32_t plo, uint32_t phi, uint32_t sweep, const RoundKeys &rk,
+                                             uint32_t t2c, uint32_t t4c, uint32_t t6c, PackedHalves &h) {
+  if constexpr (M < 32) {
+    const U4 q = philox4x32_10_rk(U4{plo + (uint32_t)M, phi, sweep, 0u}, rk);
+    constexpr int H = M >> 4;
+    constexpr uint32_t BE = 1u << (2 * (M & 15)), BO = BE << 1;
+    h.prop[H] = or_if_prop2<BO>(or_if_prop2<BE>(h.prop[H], q.x), q.z);
+    h.a2[H] = or_if_below<BO>(or_if_below<BE>(h.a2[H], q.y, t2c), q.w, t2c);
+    h.a4[H] = or_if_below<BO>(or_if_below<BE>(h.a4[H], q.y, t4c), q.w, t4c);
+    h.a6[H] = or_if_below<BO>(or_if_below<BE>(h.a6[H], q.y, t6c), q.w, t6c);
+    packed_pairs<M + 1>(plo, phi, sweep, rk, t2c, t4c, t6c, h);
+  }
+}
+
+// A threshold of 2^32 (exp(-dE/T) rounds to 1) passes every draw: its mask
+// starts all ones and the compare is made against 0.  The word's first site
+// s0 is a multiple of 64, so the pair counters plo + M never carry.
+__global__ void __launch_bounds__(256, 4) packed_draw_kernel(const PackedArgs a) {
+  const int64_t nw = a.nwords;
+  const int64_t words_per_row = a.nx >> 6;
+  const RoundKeys rk = round_keys(a.seed, kStreamSweep);
+  const bool big2 = (a.thr2 >> 32) != 0, big4 = (a.thr4 >> 32) != 0, big6 = (a.thr6 >> 32) != 0;
+  const uint32_t t2c = big2 ? 0u : (uint32_t)a.thr2, t4c = big4 ? 0u : (uint32_t)a.thr4,
+                 t6c = big6 ? 0u : (uint32_t)a.thr6;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nw; t += (int64_t)gridDim.x * blockDim.x) {
-    int64_t row = t / words_per_row;
-    int64_t w = t - row * words_per_row;
-    int64_t s0 = row * a.nx + (w << 6);  // site of bit 0 (even)
-    uint64_t prop = 0, a2 = 0, a4 = 0, a6 = 0;
-#pragma unroll 4
-    for (int m = 0; m < 32; m++) {
-      int64_t s = s0 + 2 * m;
-      U4 q = philox4x32_10(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), a.sweep, 0u}, a.seed, kStreamSweep);
-      uint64_t be = 1ull << (2 * m), bo = be << 1;
-      prop |= (q.x >= 0x7FFFFFFFu ? be : 0) | (q.z >= 0x7FFFFFFFu ? bo : 0);
-      a2 |= ((uint64_t)q.y < a.thr2 ? be : 0) | ((uint64_t)q.w < a.thr2 ? bo : 0);
-      a4 |= ((uint64_t)q.y < a.thr4 ? be : 0) | ((uint64_t)q.w < a.thr4 ? bo : 0);
-      a6 |= ((uint64_t)q.y < a.thr6 ? be : 0) | ((uint64_t)q.w < a.thr6 ? bo : 0);
+    const int64_t row = t / words_per_row;
+    const int64_t s0 = row * a.nx + ((t - row * words_per_row) << 6);  // site of bit 0
+    PackedHalves h;
+    for (int k = 0; k < 2; k++) {
+      h.prop[k] = 0;
+      h.a2[k] = big2 ? ~0u : 0u;
+      h.a4[k] = big4 ? ~0u : 0u;
+      h.a6[k] = big6 ? ~0u : 0u;
     }
+    packed_pairs<0>((uint32_t)(s0 >> 1), (uint32_t)(s0 >> 33), a.sweep, rk, t2c, t4c, t6c, h);
     PackedDecisions *D = (PackedDecisions *)a.decisions;
-    D[t] = PackedDecisions{prop, a2, a4, a6};
+    D[t] = PackedDecisions{(uint64_t)h.prop[1] << 32 | h.prop[0], (uint64_t)h.a2[1] << 32 | h.a2[0],
+                           (uint64_t)h.a4[1] << 32 | h.a4[0], (uint64_t)h.a6[1] << 32 | h.a6[0]};
   }
 }
 

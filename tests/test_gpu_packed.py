@@ -28,7 +28,8 @@ def test_pack_roundtrip_and_energy(sg):
     assert lat.energy() == oracle.energy(cfg, spin)
 
 
-@pytest.mark.parametrize("nx,ny,nz,T", [(64, 8, 6, 4.5115), (128, 4, 4, 2.2557), (64, 6, 10, 0.0), (192, 4, 2, 9.0)])
+@pytest.mark.parametrize("nx,ny,nz,T", [(64, 8, 6, 4.5115), (128, 4, 4, 2.2557), (64, 6, 10, 0.0), (192, 4, 2, 9.0),
+                                        (64, 4, 4, 1e30)])
 def test_packed_matches_oracle_and_int8(sg, nx, ny, nz, T):
     seed = 4711
     n = nx * ny * nz
