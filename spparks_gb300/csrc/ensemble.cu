@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) e
 // the previous sweep finishes: the temperature index, thresholds and ctl it
 // reads before the wait are written only by the exchange launch.
 template <bool AFTER_GRID>
-__global__ void __launch_bounds__(64, 24) ensemble_warp_kernel(EnsArgs a, int k) {
+__global__ void __launch_bounds__(64, 20) ensemble_warp_kernel(EnsArgs a, int k) {
   __shared__ __align__(16) int8_t stage[2][kWStageBytes];
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kTileThreads) fused2d_kernel(FusedArgs a) {
               (unsigned long long)w);
 }
 
-__global__ void __launch_bounds__(64, 24) fused2d_warp_kernel(FusedArgs a) {
+__global__ void __launch_bounds__(64, 20) fused2d_warp_kernel(FusedArgs a) {
   __shared__ __align__(16) int8_t stage[2][kWStageBytes];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tpr = a.nx / kTile;
