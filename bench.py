@@ -35,6 +35,7 @@ import os
 import re
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 from pathlib import Path
@@ -95,11 +96,10 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"spk_bench_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
