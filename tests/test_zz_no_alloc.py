@@ -28,12 +28,14 @@ def lib():
     return spparks_gb300.load_library()
 
 
-@pytest.mark.parametrize("app,q,T,nx,ny,sb,calls", [
-    ("ising", 2, 2.269, 64, 64, 1, (3, 4)),
-    ("potts", 30, 0.8, 96, 32, 4, (2, 3)),
-    ("potts/neighonly", 7, 0.5, 32, 64, 2, (1, 2)),
+@pytest.mark.parametrize("app,q,T,nx,ny,sb,calls,offset", [
+    ("ising", 2, 2.269, 64, 64, 1, (3, 4), 0),
+    # 8-byte but not 16-byte aligned: the 64-thread tile instead of the warp tile
+    ("ising", 2, 2.269, 96, 64, 1, (2, 3), 8),
+    ("potts", 30, 0.8, 96, 32, 4, (2, 3), 0),
+    ("potts/neighonly", 7, 0.5, 32, 64, 2, (1, 2), 0),
 ])
-def test_noalloc_matches_regular_entry_point(lib, app, q, T, nx, ny, sb, calls):
+def test_noalloc_matches_regular_entry_point(lib, app, q, T, nx, ny, sb, calls, offset):
     import torch
 
     import spparks_gb300 as sg
@@ -45,7 +47,10 @@ def test_noalloc_matches_regular_entry_point(lib, app, q, T, nx, ny, sb, calls):
     ref.set_temperature(T)
     ref.upload(spin)
     dtype = {1: torch.int8, 2: torch.int16, 4: torch.int32}[sb]
-    dev = torch.from_numpy(spin).to(dtype).cuda()
+    store = torch.zeros(n + 16, dtype=dtype).cuda()
+    dev = store[offset:offset + n]
+    dev.copy_(torch.from_numpy(spin).to(dtype).cuda())
+    assert dev.data_ptr() % 16 == (offset * dev.element_size()) % 16
     torch.cuda.synchronize()
     sweep0 = 0
     before = 0
