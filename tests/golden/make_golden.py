@@ -145,6 +145,18 @@ SWEEP_CASES = [
          temperature=0.0, seed=13, nsweeps=6, nsector=4, mask=True),
     dict(name="ising_sq4n_mask_T1", app="ising", nspins=2, lattice="sq/4n", nx=8, ny=8, nz=1,
          temperature=1.0, seed=14, nsweeps=4, mask=True),
+    # edge cases: periodic extents of 2 (a site meets the same neighbour site more than once) and Q = 1 (no
+    # site can change)
+    dict(name="ising_sq4n_2x2", app="ising", nspins=2, lattice="sq/4n", nx=2, ny=2, nz=1,
+         temperature=2.0, seed=31, nsweeps=8),
+    dict(name="potts_sq8n_2x2_Q5", app="potts", nspins=5, lattice="sq/8n", nx=2, ny=2, nz=1,
+         temperature=1.0, seed=32, nsweeps=6),
+    dict(name="neighonly_sc26n_2x2x2_Q10", app="potts/neighonly", nspins=10, lattice="sc/26n", nx=2, ny=2,
+         nz=2, temperature=0.5, seed=33, nsweeps=6),
+    dict(name="potts_sq4n_Q1", app="potts", nspins=1, lattice="sq/4n", nx=16, ny=16, nz=1,
+         temperature=1.0, seed=34, nsweeps=3),
+    dict(name="neighonly_sq8n_Q1", app="potts/neighonly", nspins=1, lattice="sq/8n", nx=8, ny=8, nz=1,
+         temperature=0.5, seed=35, nsweeps=3),
 ]
 
 KMC_CASES = [

@@ -28,7 +28,7 @@ def make_lattice(sg, case, spin_bytes=0, rng=0, seed=None, procs=(1, 1, 1)):
                       seed=case.get("seed", 0) if seed is None else seed)
 
 
-@pytest.mark.parametrize("k", range(13))
+@pytest.mark.parametrize("k", range(18))
 def test_sweeps_match_reference_fixtures(sg, ref_fixtures, k):
     fx = ref_fixtures["sweeps"][k]
     case = fx["case"]

@@ -44,7 +44,7 @@ def test_neighbor_order_matches_reference_offsets():
     assert len(nb) == 26 and nb[0] == idx(3, 3, 3) and nb[-1] == idx(1, 1, 1)
 
 
-@pytest.mark.parametrize("k", range(13))
+@pytest.mark.parametrize("k", range(18))
 def test_sweeps_match_reference(ref_fixtures, k):
     fx = ref_fixtures["sweeps"][k]
     case = fx["case"]
