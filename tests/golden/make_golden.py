@@ -166,6 +166,12 @@ KMC_CASES = [
          temperature=2.0, seed=32, runs=[2.0]),
     dict(name="kmc_potts_sc26n_8_Q50", app="potts", nspins=50, lattice="sc/26n", nx=8, ny=8, nz=8,
          temperature=0.8, seed=33, runs=[0.6]),
+    # edge cases: Q = 1 (every propensity zero: one pass, nothing changes) and a 4x4 lattice (sectors of 2x2,
+    # repeated neighbour sites)
+    dict(name="kmc_potts_sq8n_8_Q1", app="potts", nspins=1, lattice="sq/8n", nx=8, ny=8, nz=1,
+         temperature=1.0, seed=36, runs=[0.5]),
+    dict(name="kmc_potts_sq8n_4x4_Q4", app="potts", nspins=4, lattice="sq/8n", nx=4, ny=4, nz=1,
+         temperature=0.9, seed=37, runs=[1.0, 0.5]),
 ]
 
 # tree KMC with stats and energy between passes (Philox shim): the log's rows

@@ -20,7 +20,7 @@ def sg():
     return spparks_gb300
 
 
-@pytest.mark.parametrize("k", range(3))
+@pytest.mark.parametrize("k", range(5))
 def test_kmc_matches_reference_fixtures(sg, ref_fixtures, k):
     fx = ref_fixtures["kmc"][k]
     c = fx["case"]

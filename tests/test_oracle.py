@@ -59,7 +59,7 @@ def test_sweeps_match_reference(ref_fixtures, k):
     assert spin.tolist() == fx["snaps"]["final"]["spins"]
 
 
-@pytest.mark.parametrize("k", range(3))
+@pytest.mark.parametrize("k", range(5))
 def test_kmc_matches_reference(ref_fixtures, k):
     fx = ref_fixtures["kmc"][k]
     case = fx["case"]
