@@ -110,6 +110,27 @@ def test_autotuner_times_both_forms_then_caches(sg, monkeypatch):
     assert all(v is None for v in again["tune_ms"].values())  # cached: nothing timed
 
 
+def test_ensemble_extreme_temperatures(sg, mode):
+    """thresholds at both ends in every execution form: kT = 0.01 (every
+    uphill threshold 0) and 1e30 (exp(-dE/kT) rounds to 1: threshold 2^32,
+    every draw passes), with exchanges between them"""
+    L = [64, 32, 64, 32]
+    T = [0.01, 1e30, 50.0, 1.5]
+    spins = [oracle.init_spins(60 + r, l * l, 1, 2) for r, l in enumerate(L)]
+    ens = sg.Ensemble(L, T, "ising", 2, seed=12, exchange_every=2)
+    ens.upload(np.concatenate(spins))
+    orc = oracle.EnsembleOracle(L, T, "ising", 2, seed=12, every=2)
+    ref = [x.copy() for x in spins]
+    ens.run(6)
+    orc.run(ref, 6)
+    got = ens.download()
+    for r in range(len(L)):
+        assert np.array_equal(ens.replica(got, r), ref[r]), f"replica {r}"
+    assert ens.stats()["naccept"] == orc.naccept
+    assert ens.temperatures().tolist() == orc.temperatures()
+    ens.close()
+
+
 def test_ensemble_rejects_bad_sizes(sg):
     with pytest.raises(sg.SpkGpuError):
         sg.Ensemble([48], [2.0])
