@@ -119,6 +119,8 @@ struct WarpDraws {
   uint32_t ring[2];
 };
 
+// the draws of segments M0 .. M1-1 and, if RING, of the ring sites
+template <int M0, int M1, bool RING>
 __device__ __forceinline__ void warp_draws(const TileJob &j, int lane, WarpDraws &d) {
   const RoundKeys rk = round_keys(j.seed, j.key1);
   const bool big2 = (j.t2 >> 32) != 0, big4 = (j.t4 >> 32) != 0;
@@ -126,7 +128,7 @@ __device__ __forceinline__ void warp_draws(const TileJob &j, int lane, WarpDraws
   const uint32_t c0 = 0x9D9D9D9Du + 0x01010101u * ((big2 ? 1u : 0u) + (big4 ? 1u : 0u));
   // the ring first: its codes then stay live in two registers only
 #pragma unroll
-  for (int r = 0; r < 2; r++) {
+  for (int r = 0; r < (RING ? 2 : 0); r++) {
     int rlx, rly;
     warp_ring_pos(lane + 32 * r, rlx, rly);
     int gy = j.y0 + rly, gx = j.x0 + rlx;
@@ -138,7 +140,7 @@ __device__ __forceinline__ void warp_draws(const TileJob &j, int lane, WarpDraws
     d.ring[r] = add_lane_code<0>(c0 & 0xFFu, odd ? w.z : w.x, odd ? w.w : w.y, t2c, t4c);
   }
 #pragma unroll
-  for (int m = 0; m < kWSegPerLane; m++) {
+  for (int m = M0; m < M1; m++) {
     const int ly = (lane >> 2) + 8 * m;
     const int64_t s = (int64_t)(j.y0 + ly) * j.L + j.x0 + 8 * (lane & 3);
     const uint32_t plo = (uint32_t)(s >> 1), phi = (uint32_t)(s >> 33);  // plo % 4 == 0
@@ -225,21 +227,23 @@ __device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *st
 // stage, draws, then both phases of one tile; j.t2 and j.t4 are the
 // thresholds thr[2] and thr[4] (thr[2] >= thr[4]); returns this lane's changes
 // AFTER_GRID: the kernel was launched as a programmatic dependent of the
-// previous sweep, whose output this tile reads: the draws (which read no
-// site) run first, then griddepcontrol.wait holds the warp until that grid
-// has completed and its writes are visible, then the tile is staged.
+// previous sweep, whose output this tile reads: the ring's and half the
+// segments' draws (which read no site) run first, then griddepcontrol.wait
+// holds the warp until that grid has completed and its writes are visible,
+// then the tile is staged while the other half of the draws runs.
 template <bool AFTER_GRID>
 __device__ __forceinline__ unsigned int warp_tile_ising8(const TileJob &j, int8_t *stage, int lane) {
   WarpDraws d;
   if (AFTER_GRID) {
-    warp_draws(j, lane, d);
+    warp_draws<0, kWSegPerLane / 2, true>(j, lane, d);
     asm volatile("griddepcontrol.wait;\n" ::: "memory");
     warp_stage_async(j, stage, lane);
     cp_async_commit();
+    warp_draws<kWSegPerLane / 2, kWSegPerLane, false>(j, lane, d);
   } else {
     warp_stage_async(j, stage, lane);
     cp_async_commit();
-    warp_draws(j, lane, d);
+    warp_draws<0, kWSegPerLane, true>(j, lane, d);
   }
   cp_async_wait<0>();
   __syncwarp();
