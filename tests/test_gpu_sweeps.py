@@ -210,3 +210,24 @@ def test_pinned_ensemble_buffers_equal_pageable(sg):
         out.append(dst.tolist())
         ens.close()
     assert out[0] == out[1]
+
+
+@pytest.mark.parametrize("T", [2.269, 0.0, 1e30])
+def test_fused_warp_sweeps_in_one_call_match_oracle(sg, T):
+    """Ising int8 on sq/4n through the warp tile, 7 sweeps in one call, then 3
+    more in another call: equal to the oracle"""
+    seed, nx, ny = 8080, 96, 64
+    spin = oracle.init_spins(seed, nx * ny, 1, 2)
+    cfg = oracle.make_cfg("sq/4n", nx, ny, 1, "ising", 2, T, seed=seed)
+    ref = spin.copy()
+    na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 10)
+    lat = sg.Lattice("sq/4n", nx, ny, 1, "ising", 2, spin_bytes=1, seed=seed)
+    lat.set_temperature(T)
+    lat.upload(spin)
+    lat.sweep(7)
+    assert oracle.spin_hash(lat.download()) == int(hashes[6])
+    lat.sweep(3)
+    assert oracle.spin_hash(lat.download()) == int(hashes[9])
+    st = lat.stats()
+    assert (st["naccept"], st["nattempt"]) == (na, nt)
+    lat.close()
