@@ -421,8 +421,11 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) e
 // launched as a programmatic dependent (AFTER_GRID: sweeps 2.. of a group,
 // which follow a sweep kernel, never the exchange) computes its draws while
 // the previous sweep finishes: the temperature index, thresholds and ctl it
-// reads before the wait are written only by the exchange launch.
-template <bool AFTER_GRID>
+// reads before the wait are written only by the exchange launch.  BONDS (the
+// last sweep before an exchange round): the tiles also add the replica's
+// unlike bonds after the sweep to a.bonds (warp_tile_bonds), in place of
+// ensemble_bonds_kernel.
+template <bool AFTER_GRID, bool BONDS>
 __global__ void __launch_bounds__(64, 20) ensemble_warp_kernel(EnsArgs a, int k) {
   __shared__ __align__(16) int8_t stage[2][kWStageBytes];
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
@@ -450,9 +453,15 @@ __global__ void __launch_bounds__(64, 20) ensemble_warp_kernel(EnsArgs a, int k)
   j.thr = a.thr + (int64_t)j.replica * 5;
   j.t2 = j.thr[2];
   j.t4 = j.thr[4];
-  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8<AFTER_GRID>(j, stage[warp], lane));
+  unsigned int bonds = 0;
+  const unsigned int w =
+      __reduce_add_sync(0xFFFFFFFFu, warp_tile_ising8<AFTER_GRID, BONDS>(j, stage[warp], lane, &bonds));
   if (lane == 0 && w)
     atomicAdd(&a.nacc_slots[(2 * blockIdx.x + warp) & (kCounterSlots - 1)], (unsigned long long)w);
+  if (BONDS) {
+    const unsigned int b = __reduce_add_sync(0xFFFFFFFFu, bonds);
+    if (lane == 0 && b) atomicAdd(&a.bonds[r], (unsigned long long)b);
+  }
 }
 
 // unlike bonds (right and down neighbour of each site) of every replica in
@@ -597,10 +606,13 @@ static cudaError_t ens_launch(spkgpu_ensemble *e, int nsweeps) {
 }
 
 // one sweep launch of the per-sweep forms (1, 2 or 4 tiles per CTA)
-static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cudaStream_t st) {
+// (warp form: `bonds` = the last sweep before an exchange round counts the
+// replicas' unlike bonds itself)
+static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cudaStream_t st, bool bonds) {
   if (e->mode == SPKGPU_ENSEMBLE_WARPS) {
     if (k == 0) {
-      ensemble_warp_kernel<false><<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
+      if (bonds) ensemble_warp_kernel<false, true><<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
+      else ensemble_warp_kernel<false, false><<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
       return;
     }
     cudaLaunchConfig_t cfg = {};
@@ -612,7 +624,8 @@ static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cuda
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, ensemble_warp_kernel<true>, a, k);
+    if (bonds) cudaLaunchKernelEx(&cfg, ensemble_warp_kernel<true, true>, a, k);
+    else cudaLaunchKernelEx(&cfg, ensemble_warp_kernel<true, false>, a, k);
     return;
   }
   const int tpc = e->mode == SPKGPU_ENSEMBLE_LAUNCHES4 ? 4 : (e->mode == SPKGPU_ENSEMBLE_LAUNCHES2 ? 2 : 1);
@@ -633,17 +646,21 @@ static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cuda
 static cudaError_t ens_launch_group(spkgpu_ensemble *e, int m, bool exchange, int64_t *nk) {
   const EnsArgs &a = e->args;
   const unsigned nt = (unsigned)e->ntiles;
-  for (int k = 0; k < m; k++) launch_sweep(e, a, k, e->stream);
-  if (exchange) ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, e->stream>>>(a, m);
+  // the warp form counts the bonds in the last sweep of the group
+  const bool sweep_bonds = exchange && e->mode == SPKGPU_ENSEMBLE_WARPS;
+  for (int k = 0; k < m; k++) launch_sweep(e, a, k, e->stream, sweep_bonds && k == m - 1);
+  if (exchange && !sweep_bonds)
+    ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, e->stream>>>(a, m);
   ensemble_advance_kernel<<<1, 256, 0, e->stream>>>(a, m, exchange ? 1 : 0);
-  *nk += m + (exchange ? 1 : 0) + 1;
+  *nk += m + (exchange && !sweep_bonds ? 1 : 0) + 1;
   return cudaGetLastError();
 }
 
 // kernels one step (chunk sweeps) launches in the current mode
 static int64_t ens_step_kernels(const spkgpu_ensemble *e) {
   if (e->mode == SPKGPU_ENSEMBLE_PERSISTENT) return 1;
-  return e->chunk + (e->d.exchange_every > 0 ? 1 : 0) + 1;
+  const bool exchange = e->d.exchange_every > 0;
+  return e->chunk + (exchange && e->mode != SPKGPU_ENSEMBLE_WARPS ? 1 : 0) + 1;
 }
 
 // captures one step (chunk sweeps, ending on an exchange point when
@@ -669,10 +686,12 @@ static void ens_capture(spkgpu_ensemble *e) {
   } else {
     const EnsArgs &a = e->args;
     const unsigned nt = (unsigned)e->ntiles;
-    for (int k = 0; k < e->chunk; k++) launch_sweep(e, a, k, cap);
-    kev = kev && cudaEventRecordWithFlags(e->kev1, cap, cudaEventRecordExternal) == cudaSuccess;
     const bool exchange = e->d.exchange_every > 0;
-    if (exchange) ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, cap>>>(a, e->chunk);
+    const bool sweep_bonds = exchange && e->mode == SPKGPU_ENSEMBLE_WARPS;
+    for (int k = 0; k < e->chunk; k++) launch_sweep(e, a, k, cap, sweep_bonds && k == e->chunk - 1);
+    kev = kev && cudaEventRecordWithFlags(e->kev1, cap, cudaEventRecordExternal) == cudaSuccess;
+    if (exchange && !sweep_bonds)
+      ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, cap>>>(a, e->chunk);
     ensemble_advance_kernel<<<1, 256, 0, cap>>>(a, e->chunk, exchange ? 1 : 0);
     le = cudaGetLastError();
     (void)nk;

@@ -182,10 +182,58 @@ __device__ __forceinline__ uint2 warp_segment(const int8_t *stage, int c, const 
   return n;
 }
 
+// bit 7 of each byte lane set where the lane of d is non-zero
+__device__ __forceinline__ uint32_t bytes_nonzero(uint32_t d) {
+  return (((d & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | d) & 0x80808080u;
+}
+
+// Unlike bonds counted by this tile after both phases, from the stage holding
+// the tile's final values and its final colour-1 ring: every bond inside the
+// tile (right and down neighbour of each site), and every bond across the
+// tile's edge whose colour-2 end is in the tile (the other end is a ring
+// site).  Each bond across two tiles has exactly one colour-2 end, so the
+// tiles of a lattice count each unlike bond once.  This lane's share.
+__device__ __forceinline__ unsigned int warp_tile_bonds(const int8_t *stage, int lane) {
+  const int x0 = 8 * (lane & 3);
+  const bool odd_rows = (lane >> 2) & 1;  // the parity of every row of this lane
+  unsigned int b = 0;
+#pragma unroll
+  for (int m = 0; m < kWSegPerLane; m++) {
+    const int ly = (lane >> 2) + 8 * m;
+    const int c = wstage_at(x0, ly);
+    const uint2 v = *(const uint2 *)(stage + c);
+    const uint32_t rw = *(const uint32_t *)(stage + c + 8);
+    const uint32_t h_lo = bytes_nonzero(v.x ^ __funnelshift_r(v.x, v.y, 8));
+    uint32_t h_hi = bytes_nonzero(v.y ^ __funnelshift_r(v.y, rw, 8));
+    // column 31 meets column 32 outside the tile: counted where (31, y) is colour 2, y even
+    if (x0 == kTile - 8 && odd_rows) h_hi &= 0x00808080u;
+    const uint2 dn = *(const uint2 *)(stage + c + kWStageX);
+    uint32_t d_lo = bytes_nonzero(v.x ^ dn.x), d_hi = bytes_nonzero(v.y ^ dn.y);
+    // row 31 meets row 32 outside the tile: counted where (x, 31) is colour 2, x even
+    if (ly == kTile - 1) {
+      d_lo &= 0x00800080u;
+      d_hi &= 0x00800080u;
+    }
+    b += __popc(h_lo) + __popc(h_hi) + __popc(d_lo) + __popc(d_hi);
+    if (ly == 0) {  // row 0 meets row -1: counted where (x, 0) is colour 2, x odd
+      const uint2 up = *(const uint2 *)(stage + c - kWStageX);
+      b += __popc(bytes_nonzero(v.x ^ up.x) & 0x80008000u) + __popc(bytes_nonzero(v.y ^ up.y) & 0x80008000u);
+    }
+    if (x0 == 0 && odd_rows) {  // column 0 meets column -1: counted where (0, y) is colour 2, y odd
+      const uint32_t lw = *(const uint32_t *)(stage + c - 4);
+      b += ((v.x ^ (lw >> 24)) & 0xFFu) != 0;
+    }
+  }
+  return b;
+}
+
 // Both colour phases of the staged tile (warp_stage_async, waited for and
 // followed by __syncwarp); the tile's final values go to j.dst.  Returns the
-// number of this lane's sites that changed.
-__device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *stage, int lane, const WarpDraws &d) {
+// number of this lane's sites that changed; with BONDS, also this lane's
+// share of the unlike bonds after the sweep in *bonds (warp_tile_bonds).
+template <bool BONDS>
+__device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *stage, int lane, const WarpDraws &d,
+                                                    unsigned int *bonds) {
   int8_t *dst = (int8_t *)j.dst;
   const int x0 = 8 * (lane & 3);
   // colour-1 lanes have the parity of the row; rows of a lane share a parity
@@ -217,9 +265,17 @@ __device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *st
   for (int m = 0; m < kWSegPerLane; m++) {
     const int ly = (lane >> 2) + 8 * m;
     uint2 v;
-    const uint2 n = warp_segment(stage, wstage_at(x0, ly), d, m, cm2, v);
+    const int c = wstage_at(x0, ly);
+    const uint2 n = warp_segment(stage, c, d, m, cm2, v);
     cnt += (v.x ^ n.x) + (v.y ^ n.y);
     *(uint2 *)(dst + (int64_t)(j.y0 + ly) * j.L + j.x0 + x0) = n;
+    // the colour-2 lanes are final; readers of this word in this phase use
+    // only its colour-1 lanes, which do not change
+    if (BONDS) *(uint2 *)(stage + c) = n;
+  }
+  if (BONDS) {
+    __syncwarp();
+    *bonds = warp_tile_bonds(stage, lane);
   }
   return ((cnt * 0x01010101u) >> 24) / 3u;
 }
@@ -231,8 +287,9 @@ __device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *st
 // segments' draws (which read no site) run first, then griddepcontrol.wait
 // holds the warp until that grid has completed and its writes are visible,
 // then the tile is staged while the other half of the draws runs.
-template <bool AFTER_GRID>
-__device__ __forceinline__ unsigned int warp_tile_ising8(const TileJob &j, int8_t *stage, int lane) {
+template <bool AFTER_GRID, bool BONDS = false>
+__device__ __forceinline__ unsigned int warp_tile_ising8(const TileJob &j, int8_t *stage, int lane,
+                                                         unsigned int *bonds = nullptr) {
   WarpDraws d;
   if (AFTER_GRID) {
     warp_draws<0, kWSegPerLane / 2, true>(j, lane, d);
@@ -247,7 +304,7 @@ __device__ __forceinline__ unsigned int warp_tile_ising8(const TileJob &j, int8_
   }
   cp_async_wait<0>();
   __syncwarp();
-  return warp_phases(j, stage, lane, d);
+  return warp_phases<BONDS>(j, stage, lane, d, bonds);
 }
 
 }  // namespace spk
