@@ -27,7 +27,8 @@
    handle must come from one host thread at a time.
 
    Random numbers: Philox4x32-10 keyed by (seed, stream) with counter
-   (site pair, sweep, pass), as stated in spparks_gb300/csrc/spk_philox.cuh.  With
+   (site quad for ising, site pair for the other apps; sweep, pass), as stated
+   in spparks_gb300/csrc/spk_philox.cuh.  With
    SPKGPU_RNG_STRICT each site carries the reference's own Park-Miller state
    (sweep color/strict, src/app_lattice.cpp:287-295, 796-805) instead. */
 #ifndef SPKGPU_H
@@ -179,9 +180,10 @@ int spkgpu_kmc_run_until(spkgpu_lattice *h, double *time, double stoptime, doubl
 /* integer-issue ceiling ------------------------------------------------------
    No counterpart in the reference.  Philox4x32-10 blocks per second that
    device computes with the sweep kernels' own Philox code and nothing else
-   (iters blocks x 4 per thread, 8 CTAs of 128 threads per SM); a sweep
-   spends one block per x-pair of sites, so 2 x this rate bounds every sweep
-   of the Philox draw contract. */
+   (iters blocks x 4 per thread, 8 CTAs of 128 threads per SM); an ising
+   sweep spends one block per four sites and the other apps one per x-pair,
+   so 4 x (ising) or 2 x (the others) this rate bounds every sweep of the
+   Philox draw contract. */
 int spkgpu_philox_rate(int32_t device, int32_t iters, double *blocks_per_s);
 
 /* sweeping without allocating ----------------------------------------------

@@ -17,8 +17,12 @@
      replica exchange round k, group g, slot pair j:
        counter = { k, g, j, 0 }, word 0
      rejection sweep, site s = id-1 (0-based), sweep n, pass p within sweep:
-       counter = { s>>1 (low 32), s>>33, n, p }, draw d of site s uses
-       word 2*(s&1)+d  (two sites share one Philox block; d is 0 or 1)
+       potts, potts/neighonly, potts/neigh: counter = { s>>1 (low 32), s>>33,
+       n, p }, draw d of site s uses word 2*(s&1)+d  (two sites share one
+       Philox block; d is 0 or 1)
+       ising: counter = { s>>2 (low 32), s>>34, n, p }, site s takes the one
+       word x = word s&3 (four sites share one block); draw 0 is
+       u0 = (2*(x>>31) + 1) / 4 and draw 1 is u1 = ((x & 0x7FFFFFFF) + 1) 2^-31
      KMC event k of chain c:  counter = { c, k low, k high, 0 }; word 0 is
        the tree pick, word 1 the clock, word 2 the event choice
      initial spin of site s: counter = { s>>1, s>>33, 0, 0 }, word 2*(s&1)
@@ -59,7 +63,7 @@ static inline void spko_philox4x32_10(const uint32_t ctr[4], const uint32_t key[
   out[3] = c3;
 }
 
-/* the two draws of site s in sweep n, pass p */
+/* the two draws of site s in sweep n, pass p (apps other than ising) */
 static inline void spko_site_draws(uint32_t seed, uint32_t stream_base, uint64_t s, uint32_t sweep,
                                    uint32_t pass, uint32_t *x0, uint32_t *x1) {
   uint32_t ctr[4] = {(uint32_t)(s >> 1), (uint32_t)(s >> 33), sweep, pass};
@@ -69,6 +73,23 @@ static inline void spko_site_draws(uint32_t seed, uint32_t stream_base, uint64_t
   int h = (int)(s & 1) * 2;
   *x0 = w[h];
   *x1 = w[h + 1];
+}
+
+/* the one word of ising site s in sweep n, pass p */
+static inline uint32_t spko_ising_word(uint32_t seed, uint32_t stream_base, uint64_t s, uint32_t sweep,
+                                       uint32_t pass) {
+  uint32_t ctr[4] = {(uint32_t)(s >> 2), (uint32_t)(s >> 34), sweep, pass};
+  uint32_t key[2] = {seed, stream_base | SPKO_STREAM_SWEEP};
+  uint32_t w[4];
+  spko_philox4x32_10(ctr, key, w);
+  return w[s & 3];
+}
+
+/* the ising site's two uniforms from its word: the proposal from the top bit,
+   the Boltzmann draw from the low 31 bits (both exact in double) */
+static inline double spko_ising_u0(uint32_t x) { return (2.0 * (double)(x >> 31) + 1.0) * 0.25; }
+static inline double spko_ising_u1(uint32_t x) {
+  return ((double)(x & 0x7FFFFFFFu) + 1.0) * (1.0 / 2147483648.0);
 }
 
 static inline void spko_kmc_draws(uint32_t seed, uint32_t chain, uint64_t k, uint32_t w[4]) {

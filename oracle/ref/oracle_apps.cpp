@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "oracle_apps.h"
 #include "oracle_solve.h"
@@ -46,13 +47,18 @@ void PhiloxApp<Base>::site_event_rejection(int i, RandomPark *random) {
     visits.assign(this->nlocal, 0);
     visits_sweep = this->nsweeps;
   }
+  // ising: one word per site, four sites per block; the other apps: two
+  // words per site, two sites per block
+  const bool ising = std::is_same<Base, AppIsing>::value;
   uint64_t s = (uint64_t)(this->id[i] - 1);
-  uint32_t ctr[4] = {(uint32_t)(s >> 1), (uint32_t)(s >> 33), (uint32_t)this->nsweeps,
+  const int sh = ising ? 2 : 1;
+  uint32_t ctr[4] = {(uint32_t)(s >> sh), (uint32_t)(s >> (32 + sh)), (uint32_t)this->nsweeps,
                      (uint32_t)visits[i]};
   uint32_t key[2] = {spk_shim::philox_seed, SPKO_STREAM_SWEEP};
   spk_shim::DrawCtx &c = spk_shim::ctx;
   spko_philox4x32_10(ctr, key, c.w);
-  c.base = (int)(s & 1) * 2;
+  c.base = ising ? (int)(s & 3) : (int)(s & 1) * 2;
+  c.ising = ising ? 1 : 0;
   c.next = 0;
   c.limit = 2;
   c.active = 1;
@@ -70,6 +76,7 @@ void PhiloxApp<Base>::site_event(int i, RandomPark *random) {
   spk_shim::DrawCtx &c = spk_shim::ctx;
   memcpy(c.w, spk_oracle::last_event_words, sizeof(c.w));
   c.base = 2;
+  c.ising = 0;
   c.next = 0;
   c.limit = 1;
   c.active = 1;
@@ -114,6 +121,7 @@ int SolveTreePhilox::event(double *pdt) {
   spko_kmc_draws(spk_shim::philox_seed, chain, nevent, c.w);
   nevent++;
   c.base = 0;
+  c.ising = 0;
   c.next = 0;
   c.limit = 2;
   c.active = 1;

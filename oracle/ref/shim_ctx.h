@@ -13,6 +13,7 @@ struct DrawCtx {
   int base;        // first word this context may hand out
   int next;        // draws handed out so far
   int limit;       // draws allowed
+  int ising;       // 1: both draws come from word `base` (ising sweeps)
 };
 
 extern DrawCtx ctx;

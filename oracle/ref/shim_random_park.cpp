@@ -3,7 +3,9 @@
 
    While a draw context is open (set by the oracle app and solver subclasses
    in oracle_apps.cpp around one site update or one KMC event), uniform()
-   returns the next Philox word of that context as u = (x+1) * 2^-32.
+   returns the next Philox word of that context as u = (x+1) * 2^-32; in an
+   ising sweep both draws come from the site's one word x, the first as
+   (2*(x>>31) + 1) / 4 and the second as ((x & 0x7FFFFFFF) + 1) * 2^-31.
    Otherwise it runs the reference's Park-Miller minimal-standard recurrence
    (IA=16807, IM=2^31-1, Schrage factorisation with IQ=127773, IR=2836), so
    that every other consumer (set site range, solver construction) behaves as
@@ -20,7 +22,7 @@
 using namespace SPPARKS_NS;
 
 namespace spk_shim {
-DrawCtx ctx = {0, {0, 0, 0, 0}, 0, 0, 0};
+DrawCtx ctx = {0, {0, 0, 0, 0}, 0, 0, 0, 0};
 uint32_t philox_seed = 12345;
 }  // namespace spk_shim
 
@@ -57,6 +59,11 @@ double RandomPark::uniform() {
     if (c.next >= c.limit) {
       fprintf(stderr, "oracle shim: draw %d requested, context allows %d\n", c.next, c.limit);
       exit(3);
+    }
+    if (c.ising) {
+      uint32_t x = c.w[c.base];
+      return c.next++ == 0 ? (2.0 * (double)(x >> 31) + 1.0) * 0.25
+                           : ((double)(x & 0x7FFFFFFFu) + 1.0) * (1.0 / 2147483648.0);
     }
     uint32_t x = c.w[c.base + c.next];
     c.next++;

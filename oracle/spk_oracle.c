@@ -286,6 +286,7 @@ void spko_set_range(int32_t park_seed, int64_t n, int lo, int hi, int32_t *spin)
 typedef struct {
   int mode;          /* SPKO_RNG_PHILOX / SPKO_RNG_STRICT */
   uint32_t x[2];     /* Philox words of this site update */
+  int ising;         /* x[0] is the ising site's one word (both draws) */
   int used;
   int32_t *park;     /* strict: the site's Park-Miller state */
 } draw_src;
@@ -295,6 +296,11 @@ static double draw_uniform(draw_src *d) {
   if (d->used >= 2) {
     fprintf(stderr, "oracle: more than two draws in one site update\n");
     abort();
+  }
+  if (d->ising) {
+    double u = d->used == 0 ? spko_ising_u0(d->x[0]) : spko_ising_u1(d->x[0]);
+    d->used++;
+    return u;
   }
   return spko_u(d->x[d->used++]);
 }
@@ -441,10 +447,15 @@ int spko_color_sweeps(const spko_cfg *c, int32_t *spin, int64_t sweep0, int nswe
               draw_src d;
               d.mode = c->rng;
               d.used = 0;
+              d.ising = 0;
               d.park = siteseeds ? &siteseeds[i] : NULL;
-              if (c->rng == SPKO_RNG_PHILOX)
+              if (c->rng == SPKO_RNG_PHILOX && c->app == SPKO_ISING) {
+                d.x[0] = d.x[1] = spko_ising_word(c->seed, c->stream_base, (uint64_t)i, sweep, (uint32_t)p);
+                d.ising = 1;
+              } else if (c->rng == SPKO_RNG_PHILOX) {
                 spko_site_draws(c->seed, c->stream_base, (uint64_t)i, sweep, (uint32_t)p, &d.x[0],
                                 &d.x[1]);
+              }
               *naccept += site_event_rejection_nb(c, spin, i, nbt + i * nn, nn, &d, mask);
             }
           }
@@ -494,6 +505,7 @@ int spko_random_sector_sweeps(const spko_cfg *c, int32_t *spin, int32_t *ranapp,
         draw_src d;
         d.mode = SPKO_RNG_STRICT;
         d.used = 0;
+        d.ising = 0;
         d.park = ranapp;
         *naccept += site_event_rejection(c, spin, sitelist[k], &d, NULL);
       }

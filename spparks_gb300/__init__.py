@@ -179,7 +179,8 @@ def load_library(path: Path | None = None):
 
 def philox_rate(device: int = 0, iters: int = 4096) -> float:
     """Philox4x32-10 blocks/s of the device with the sweeps' own code
-    (spkgpu_philox_rate): half the draw-side ceiling of any sweep."""
+    (spkgpu_philox_rate): a quarter of the draw-side ceiling of an Ising
+    sweep (four sites per block), half that of the other apps."""
     lib = load_library()
     v = ctypes.c_double()
     rc = lib.spkgpu_philox_rate(int(device), int(iters), ctypes.byref(v))

@@ -897,7 +897,7 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   std::vector<double> beta(n);
   for (int t = 0; t < n; t++) {
     AcceptTable at;
-    build_accept_table(e->T0[t], &at);
+    build_accept_table(e->T0[t], e->d.app, &at);
     for (int k = 0; k < 5; k++) thr[(size_t)t * 5 + k] = at.thr[k];
     beta[t] = 1.0 / e->T0[t];
   }

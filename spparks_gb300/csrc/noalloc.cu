@@ -94,7 +94,7 @@ extern "C" int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int3
   f.seed = seed;
   f.nspins = nspins;
   f.naccept = counter;
-  spk::build_accept_table(temperature, &f.acc);
+  spk::build_accept_table(temperature, app, &f.acc);
   for (int32_t k = 0; k < nsweeps; k++) {
     f.src = (k & 1) ? other : spin;
     f.dst = (k & 1) ? spin : other;

@@ -5,12 +5,13 @@
 // src/lattice.cpp:256-260), so the lattices are bit-identical.
 //
 // Per sweep:
-//   packed_draw_kernel   one thread per word computes the Philox block of
-//                        each of its 32 x-pairs once and stores, for all 64
-//                        sites, four decision masks: the proposal (draw 0 >=
-//                        2^31-1 proposes value 2) and "draw 1 < thr[dE]" for
-//                        the three uphill moves dE = 2, 4, 6; each bit is a
-//                        32-bit compare and a predicated OR.
+//   packed_draw_kernel   one thread per word computes the Philox blocks of
+//                        its 64 sites (16 blocks, four sites each) once and
+//                        stores four decision masks: the proposal (a site
+//                        word x >= 2^31 proposes value 2) and "y < thr[dE]"
+//                        (y = x & 0x7FFFFFFF) for the three uphill moves
+//                        dE = 2, 4, 6; each bit is a 32-bit compare and a
+//                        predicated OR.
 //   packed_phase_kernel  per colour, one thread per word: the unlike count of
 //                        every site against its six neighbours as a
 //                        bit-sliced 3-bit sum of XOR masks; a site of the
@@ -33,11 +34,11 @@ struct PackedDecisions {
   uint64_t prop, a2, a4, a6;
 };
 
-// c | BIT if x >= 2^31-1 (draw 0 proposes value 2), as a compare and a
-// predicated OR of an immediate
+// c | BIT if x >= 2^31 (the site's word proposes value 2), as a compare and
+// a predicated OR of an immediate
 template <uint32_t BIT>
 __device__ __forceinline__ uint32_t or_if_prop2(uint32_t c, uint32_t x) {
-  asm("{\n\t.reg .pred q;\n\tsetp.ge.u32 q, %1, 0x7FFFFFFF;\n\t@q or.b32 %0, %0, %2;\n\t}"
+  asm("{\n\t.reg .pred q;\n\tsetp.ge.u32 q, %1, 0x80000000;\n\t@q or.b32 %0, %0, %2;\n\t}"
       : "+r"(c)
       : "r"(x), "n"(BIT));
   return c;
@@ -57,44 +58,46 @@ struct PackedHalves {
   uint32_t prop[2], a2[2], a4[2], a6[2];
 };
 
-// x-pair M (sites 2M, 2M+1 of the word) and the pairs after it; the pair
+// the decision bits BIT of one site with Philox word x
+template <uint32_t BIT, int H>
+__device__ __forceinline__ void packed_site(PackedHalves &h, uint32_t x, uint32_t t2, uint32_t t4, uint32_t t6) {
+  h.prop[H] = or_if_prop2<BIT>(h.prop[H], x);
+  const uint32_t y = x & kIsingAcceptMask;
+  h.a2[H] = or_if_below<BIT>(h.a2[H], y, t2);
+  h.a4[H] = or_if_below<BIT>(h.a4[H], y, t4);
+  h.a6[H] = or_if_below<BIT>(h.a6[H], y, t6);
+}
+
+// block M (sites 4M .. 4M+3 of the word) and the blocks after it; the block
 // index is a template argument so that every mask bit is an immediate
 template <int M>
-__device__ __forceinline__ void packed_pairs(uint32_t plo, uint32_t phi, uint32_t sweep, const RoundKeys &rk,
-                                             uint32_t t2c, uint32_t t4c, uint32_t t6c, PackedHalves &h) {
-  if constexpr (M < 32) {
-    const U4 q = philox4x32_10_rk(U4{plo + (uint32_t)M, phi, sweep, 0u}, rk);
-    constexpr int H = M >> 4;
-    constexpr uint32_t BE = 1u << (2 * (M & 15)), BO = BE << 1;
-    h.prop[H] = or_if_prop2<BO>(or_if_prop2<BE>(h.prop[H], q.x), q.z);
-    h.a2[H] = or_if_below<BO>(or_if_below<BE>(h.a2[H], q.y, t2c), q.w, t2c);
-    h.a4[H] = or_if_below<BO>(or_if_below<BE>(h.a4[H], q.y, t4c), q.w, t4c);
-    h.a6[H] = or_if_below<BO>(or_if_below<BE>(h.a6[H], q.y, t6c), q.w, t6c);
-    packed_pairs<M + 1>(plo, phi, sweep, rk, t2c, t4c, t6c, h);
+__device__ __forceinline__ void packed_blocks(U4 ctr, const RoundKeys &rk, uint32_t t2, uint32_t t4, uint32_t t6,
+                                              PackedHalves &h) {
+  if constexpr (M < 16) {
+    const U4 q = philox4x32_10_rk(U4{ctr.x + (uint32_t)M, ctr.y, ctr.z, ctr.w}, rk);
+    constexpr int H = M >> 3;
+    constexpr uint32_t B = 1u << (4 * (M & 7));
+    packed_site<B, H>(h, q.x, t2, t4, t6);
+    packed_site<(B << 1), H>(h, q.y, t2, t4, t6);
+    packed_site<(B << 2), H>(h, q.z, t2, t4, t6);
+    packed_site<(B << 3), H>(h, q.w, t2, t4, t6);
+    packed_blocks<M + 1>(ctr, rk, t2, t4, t6, h);
   }
 }
 
-// A threshold of 2^32 (exp(-dE/T) rounds to 1) passes every draw: its mask
-// starts all ones and the compare is made against 0.  The word's first site
-// s0 is a multiple of 64, so the pair counters plo + M never carry.
+// Every threshold is at most 2^31, so the tests are 32-bit compares.  The
+// word's first site s0 is a multiple of 64, so the block counters
+// (s0 >> 2) + M never carry.
 __global__ void __launch_bounds__(256, 4) packed_draw_kernel(const PackedArgs a) {
   const int64_t nw = a.nwords;
   const int64_t words_per_row = a.nx >> 6;
   const RoundKeys rk = round_keys(a.seed, kStreamSweep);
-  const bool big2 = (a.thr2 >> 32) != 0, big4 = (a.thr4 >> 32) != 0, big6 = (a.thr6 >> 32) != 0;
-  const uint32_t t2c = big2 ? 0u : (uint32_t)a.thr2, t4c = big4 ? 0u : (uint32_t)a.thr4,
-                 t6c = big6 ? 0u : (uint32_t)a.thr6;
+  const uint32_t t2 = (uint32_t)a.thr2, t4 = (uint32_t)a.thr4, t6 = (uint32_t)a.thr6;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nw; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = t / words_per_row;
     const int64_t s0 = row * a.nx + ((t - row * words_per_row) << 6);  // site of bit 0
-    PackedHalves h;
-    for (int k = 0; k < 2; k++) {
-      h.prop[k] = 0;
-      h.a2[k] = big2 ? ~0u : 0u;
-      h.a4[k] = big4 ? ~0u : 0u;
-      h.a6[k] = big6 ? ~0u : 0u;
-    }
-    packed_pairs<0>((uint32_t)(s0 >> 1), (uint32_t)(s0 >> 33), a.sweep, rk, t2c, t4c, t6c, h);
+    PackedHalves h = {};
+    packed_blocks<0>(ising_counter((uint64_t)s0, a.sweep, 0u), rk, t2, t4, t6, h);
     PackedDecisions *D = (PackedDecisions *)a.decisions;
     D[t] = PackedDecisions{(uint64_t)h.prop[1] << 32 | h.prop[0], (uint64_t)h.a2[1] << 32 | h.a2[0],
                            (uint64_t)h.a4[1] << 32 | h.a4[0], (uint64_t)h.a6[1] << 32 | h.a6[0]};

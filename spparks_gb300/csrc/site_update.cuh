@@ -95,6 +95,27 @@ __device__ __forceinline__ int count_unlike(int v, const int (&nb)[NN]) {
   return e;
 }
 
+// Philox counter of the block holding site s's draws, and the draws x0
+// (proposal) and x1 (Boltzmann test) of site s from that block: ising takes
+// one word per site (x1 = its low 31 bits), the other apps two words of the
+// x-pair's block.  Two sites s, s+1 with s even share one block in both.
+template <int APP>
+SPK_HD U4 sweep_counter(uint64_t s, uint32_t sweep, uint32_t pass) {
+  return APP == SPKGPU_ISING ? ising_counter(s, sweep, pass)
+                             : U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), sweep, pass};
+}
+
+template <int APP>
+SPK_HD void site_words(const U4 &w, uint64_t s, uint32_t &x0, uint32_t &x1) {
+  if (APP == SPKGPU_ISING) {
+    x0 = block_word(w, (int)(s & 3));
+    x1 = x0 & kIsingAcceptMask;
+  } else {
+    x0 = (s & 1) ? w.z : w.x;
+    x1 = (s & 1) ? w.w : w.y;
+  }
+}
+
 // Philox form: x0 = draw 0 (proposal), x1 = draw 1 (Boltzmann test).
 // thr[dE] in shared or register memory.  At zero temperature every thr[dE]
 // is 0, so "x1 < thr" rejects every uphill move, which is the reference's
@@ -107,7 +128,7 @@ __device__ __forceinline__ int update_philox(int own, const int (&nb)[NN], uint3
   *e0_out = e0;
   int news;
   if (APP == SPKGPU_ISING) {
-    news = (x0 < 0x7FFFFFFFu) ? 1 : 2;
+    news = (x0 < kIsingProposal1) ? 1 : 2;
   } else if (APP == SPKGPU_POTTS) {
     uint32_t r = scaled_pick((uint32_t)nspins, x0);
     if (r > (uint32_t)(nspins - 1)) r = nspins - 1;

@@ -38,15 +38,16 @@ inline bool is2d(int lattice) { return lattice == SPKGPU_SQ_4N || lattice == SPK
 // Boltzmann acceptance tables for one temperature: for an energy increase
 // dE > 0 the reference rejects when u > exp((einitial-efinal)*t_inverse)
 // (src/app_ising.cpp:120); thr[dE] = floor(exp(-dE*t_inverse) * 2^32) turns
-// that into "accept iff x < thr[dE]" on the Philox word, pexp[dE] is the
-// double itself for the Park-Miller (strict) path.
+// that into "accept iff x < thr[dE]" on the Philox word (for ising,
+// floor(exp(-dE*t_inverse) * 2^31) against the word's low 31 bits), pexp[dE]
+// is the double itself for the Park-Miller (strict) path.
 struct AcceptTable {
   uint64_t thr[kMaxNeigh + 1];
   double pexp[kMaxNeigh + 1];
   int zero_t;  // temperature == 0: every uphill move is rejected
 };
 
-void build_accept_table(double temperature, AcceptTable *t);
+void build_accept_table(double temperature, int app, AcceptTable *t);
 
 // one set of sites swept in one launch: the sites of colour `color` whose
 // coordinates lie in the per-axis lists.  Every lattice colour fixes the

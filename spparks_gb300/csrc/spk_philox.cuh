@@ -6,8 +6,15 @@
 //   key      = { seed, stream }; stream 0 = rejection sweeps, 1 = KMC events,
 //              2 = replica exchange, 3 = initial spins
 //   sweep:   site s (= id-1), sweep n, pass p (0..nloop-1 within the sweep)
-//            counter = { s>>1, s>>33, n, p }; draw d of site s is word
-//            2*(s&1)+d, so the two sites of an x-pair share one block
+//            potts, potts/neighonly, potts/neigh: counter = { s>>1, s>>33,
+//            n, p }; draw d of site s is word 2*(s&1)+d, so the two sites of
+//            an x-pair share one block
+//            ising: counter = { s>>2, s>>34, n, p }; site s takes the one
+//            word x = word s&3, so four sites share one block.  Its proposal
+//            is the top bit and its Boltzmann draw the low 31 bits:
+//              draw 0 u0 = (2*(x>>31) + 1) / 4        (u0 < 0.5 <=> x < 2^31)
+//              draw 1 u1 = ((x & 0x7FFFFFFF) + 1) * 2^-31
+//            u1 has the 31-bit resolution of RandomPark's own values
 //   KMC:     event k of chain c: counter = { c, k, k>>32, 0 }; word 0 picks
 //            the tree leaf, word 1 is the clock, word 2 the event choice
 //   init:    site s: counter = { s>>1, s>>33, 0, 0 }, word 2*(s&1)
@@ -16,6 +23,8 @@
 //     u < 0.5                 <=>  x < 2^31 - 1
 //     (int)(Q*u)              ==   (Q*(x+1)) >> 32        (Q < 2^21)
 //     u > exp(-dE/T) (reject) <=>  x >= floor(exp(-dE/T) * 2^32)
+//   and for the Ising split, with y = x & 0x7FFFFFFF,
+//     u1 > exp(-dE/T) (reject) <=> y >= floor(exp(-dE/T) * 2^31)
 #pragma once
 
 #include <stdint.h>
@@ -106,11 +115,16 @@ SPK_HD U4 philox4x32_10_rk(U4 c, const RoundKeys &rk) {
   return c;
 }
 
-// Philox block of the x-pair holding site s in sweep n, pass p
-SPK_HD U4 sweep_block(uint32_t seed, uint64_t s, uint32_t sweep, uint32_t pass) {
-  U4 c{(uint32_t)(s >> 1), (uint32_t)(s >> 33), sweep, pass};
-  return philox4x32_10(c, seed, kStreamSweep);
+constexpr uint32_t kIsingProposal1 = 0x80000000u;  // x below it proposes value 1
+constexpr uint32_t kIsingAcceptMask = 0x7FFFFFFFu;  // the Boltzmann draw of x
+
+// counter of the Philox block holding the word of Ising site s
+SPK_HD U4 ising_counter(uint64_t s, uint32_t sweep, uint32_t pass) {
+  return U4{(uint32_t)(s >> 2), (uint32_t)(s >> 34), sweep, pass};
 }
+
+// word k (0..3) of a block
+SPK_HD uint32_t block_word(const U4 &w, int k) { return k == 0 ? w.x : (k == 1 ? w.y : (k == 2 ? w.z : w.w)); }
 
 SPK_HD U4 kmc_block(uint32_t seed, uint32_t chain, uint64_t k) {
   U4 c{chain, (uint32_t)k, (uint32_t)(k >> 32), 0u};

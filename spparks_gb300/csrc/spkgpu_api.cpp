@@ -48,7 +48,9 @@ int spk_cuda_fail(spkgpu_lattice *h, cudaError_t e, const char *what) {
 
 namespace spk {
 
-void build_accept_table(double temperature, AcceptTable *t) {
+void build_accept_table(double temperature, int app, AcceptTable *t) {
+  // the Boltzmann draw has 31 bits for ising, 32 for the other apps
+  const double scale = (app == SPKGPU_ISING) ? 2147483648.0 : 4294967296.0;
   t->zero_t = (temperature == 0.0) ? 1 : 0;
   double t_inverse = (temperature != 0.0) ? 1.0 / temperature : 0.0;
   for (int de = 0; de <= kMaxNeigh; de++) {
@@ -56,9 +58,9 @@ void build_accept_table(double temperature, AcceptTable *t) {
     // einitial-efinal = -dE exactly (integer-valued doubles)
     double p = exp((double)(-de) * t_inverse);
     t->pexp[de] = p;
-    double scaled = p * 4294967296.0;  // exact: power-of-two scaling
+    double scaled = p * scale;  // exact: power-of-two scaling
     double fl = floor(scaled);
-    t->thr[de] = (fl >= 4294967296.0) ? 4294967296ULL : (uint64_t)fl;
+    t->thr[de] = (fl >= scale) ? (uint64_t)scale : (uint64_t)fl;
   }
   if (t->zero_t) {
     for (int de = 0; de <= kMaxNeigh; de++) {
@@ -178,7 +180,7 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
   h->n = (int64_t)d.nx * d.ny * d.nz;
   h->ncolors = spk::ncolors_of(d.lattice);
   h->maxneigh = spk::maxneigh_of(d.lattice);
-  spk::build_accept_table(0.0, &h->acc);
+  spk::build_accept_table(0.0, d.app, &h->acc);
   int code = SPKGPU_OK;
   auto fail = [&](int c) {
     code = c;
@@ -277,7 +279,7 @@ int spkgpu_set_temperature(spkgpu_lattice *h, double temperature) {
     return spk_fail(h, SPKGPU_ERR_ARG, "temperature must be finite and >= 0");
   h->temperature = temperature;
   h->have_temperature = true;
-  spk::build_accept_table(temperature, &h->acc);
+  spk::build_accept_table(temperature, h->d.app, &h->acc);
   return SPKGPU_OK;
 }
 

@@ -59,9 +59,9 @@ __global__ void __launch_bounds__(256) phase_kernel(PhaseArgs a) {
     }
     int news, e0;
     if (a.rng == SPKGPU_RNG_PHILOX) {
-      U4 w = sweep_block(a.seed, (uint64_t)i, a.sweep, a.pass);
-      uint32_t x0 = (i & 1) ? w.z : w.x;
-      uint32_t x1 = (i & 1) ? w.w : w.y;
+      U4 w = philox4x32_10(sweep_counter<APP>((uint64_t)i, a.sweep, a.pass), a.seed, kStreamSweep);
+      uint32_t x0, x1;
+      site_words<APP>(w, (uint64_t)i, x0, x1);
       news = update_philox<NN, APP>(own, nb, x0, x1, a.nspins, thr, &e0);
     } else {
       int pm = a.siteseeds[i];

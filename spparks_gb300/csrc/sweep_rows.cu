@@ -126,11 +126,9 @@ __global__ void __launch_bounds__(512) row_pair_kernel(RowArgs a) {
       uint32_t x0, x1;
       if (half == 0) {
         int64_t s = rowbase + 2 * p;
-        U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), a.sweep, 0u}, rk);
-        x0 = w.x;
-        x1 = w.y;
-        keep0 = w.z;
-        keep1 = w.w;
+        U4 w = philox4x32_10_rk(sweep_counter<APP>((uint64_t)s, a.sweep, 0u), rk);
+        site_words<APP>(w, (uint64_t)s, x0, x1);
+        site_words<APP>(w, (uint64_t)s + 1, keep0, keep1);
       } else {
         x0 = keep0;
         x1 = keep1;

@@ -9,12 +9,13 @@
 // its post-phase state.  The tile is read from `src` and written to `dst`
 // (double buffering), so tiles never observe each other's writes.
 //
-// The Philox block of an x-pair is computed once per sweep and serves the
-// colour-1 site of the pair in the first phase and the colour-2 site in the
-// second.  A tile has 64 threads and each owns eight x-pairs: for Ising on
-// int8 site values they are two 8-site row segments, updated as eight byte
-// lanes of a 64-bit word (tile_segments_ising8); otherwise eight pairs of
-// one column updated site by site (tile_pairs_sq4).  With 64 threads every
+// The Philox block of a site is computed once per sweep and serves the
+// colour-1 sites it holds in the first phase and the colour-2 sites in the
+// second (an x-pair shares a block; for Ising, four sites do).  A tile has 64
+// threads and each owns eight x-pairs: for Ising on int8 site values they are
+// two 8-site row segments (two blocks each), updated as eight byte lanes of a
+// 64-bit word (tile_segments_ising8); otherwise eight pairs of one column
+// updated site by site (tile_pairs_sq4).  With 64 threads every
 // thread also updates exactly one ring site, so the first phase is balanced.
 #pragma once
 
@@ -129,8 +130,9 @@ __device__ __forceinline__ void ring_site(const TileJob &j, S *stage, const Roun
   gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
   gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
   int64_t s = j.base + (int64_t)gy * j.L + gx;
-  U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), j.sweep, 0u}, rk);
-  uint32_t a0 = (s & 1) ? w.z : w.x, a1 = (s & 1) ? w.w : w.y;
+  U4 w = philox4x32_10_rk(sweep_counter<APP>((uint64_t)s, j.sweep, 0u), rk);
+  uint32_t a0, a1;
+  site_words<APP>(w, (uint64_t)s, a0, a1);
   site4<APP, S>(stage, rlx, rly, a0, a1, j.nspins, j.thr);
 }
 
@@ -150,11 +152,11 @@ __device__ __forceinline__ int tile_pairs_sq4(const TileJob &j, S *stage) {
     int p = tid + k * kTileThreads;
     int ly = p >> 4, m = p & 15;
     int64_t s = j.base + (int64_t)(j.y0 + ly) * j.L + j.x0 + 2 * m;  // even
-    U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), j.sweep, 0u}, rk);
+    U4 w = philox4x32_10_rk(sweep_counter<APP>((uint64_t)s, j.sweep, 0u), rk);
     int h = ly & 1;  // which site of the pair is colour 1
-    uint32_t a0 = h ? w.z : w.x, a1 = h ? w.w : w.y;
-    keep0[k] = h ? w.x : w.z;
-    keep1[k] = h ? w.y : w.w;
+    uint32_t a0, a1;
+    site_words<APP>(w, (uint64_t)(s + h), a0, a1);
+    site_words<APP>(w, (uint64_t)(s + 1 - h), keep0[k], keep1[k]);
     changed += site4<APP, S>(stage, 2 * m + h, ly, a0, a1, j.nspins, j.thr);
   }
   if (tid < kRing) ring_site<APP, S>(j, stage, rk, tid);
@@ -187,11 +189,12 @@ __device__ __forceinline__ int tile_pairs_sq4(const TileJob &j, S *stage) {
 // 2) tells the two states apart, so the number of unlike neighbours e0 is the
 // sum of four XORs of bit 0, at most 4 per lane (no carry between lanes).
 // AppIsing::site_event_rejection (src/app_ising.cpp:104-136) then reads:
-// draw 0 proposes value 1 iff x0 < 2^31-1; a proposal equal to the current
-// value changes nothing; otherwise e1 = 4 - e0, the flip is taken iff
-// e1 <= e0 (e0 >= 2) or x1 < thr[e1-e0] with e1-e0 = 2 (e0 = 1) or 4
-// (e0 = 0).  Each site's draws are folded into a lane code
-//   lvl + 4*p,  lvl = [x1 < thr[4]] + [x1 < thr[2]],  p = [x0 < 2^31-1]
+// the site's word x proposes value 1 iff x < 2^31; a proposal equal to the
+// current value changes nothing; otherwise e1 = 4 - e0, the flip is taken iff
+// e1 <= e0 (e0 >= 2) or y < thr[e1-e0] (y = x & 0x7FFFFFFF, thr <= 2^31)
+// with e1-e0 = 2 (e0 = 1) or 4 (e0 = 0).  Each site's word is folded into a
+// lane code
+//   lvl + 4*p,  lvl = [y < thr[4]] + [y < thr[2]],  p = [x < 2^31]
 // (thr[4] <= thr[2], so lvl >= 2 - e0 <=> the Boltzmann test passes for that
 // e0), and the flip condition becomes e0 + lvl >= 2 and p != bit 0, both
 // evaluated for all lanes at once.  At zero temperature thr[] is all zero,
@@ -200,20 +203,14 @@ constexpr uint64_t kLaneBit = 0x0101010101010101ull;
 constexpr uint64_t kEvenLanes = 0x0001000100010001ull;  // bit 0 of lanes 0, 2, 4, 6
 constexpr uint64_t kOddLanes = 0x0100010001000100ull;   // bit 0 of lanes 1, 3, 5, 7
 constexpr int kSegPerThread = kTile * kTile / 8 / kTileThreads;  // 8-site segments
-static_assert(kSegPerThread * 4 == kPairsPerThread, "a segment holds four x-pairs");
+static_assert(kSegPerThread * 4 == kPairsPerThread, "a segment holds two Philox blocks of four sites");
 static_assert(kSegPerThread * 8 * kTileThreads == kTile * kTile, "segments must cover the tile");
 
-// lane code of one site from its two draws; T32: both thresholds are below
-// 2^32 (every finite temperature whose exp(-2/T) rounds below 1), so the
-// tests are 32-bit compares
-template <bool T32>
-__device__ __forceinline__ uint32_t ising_lane_code(uint32_t x0, uint32_t x1, uint64_t t2, uint64_t t4) {
-  uint32_t lvl;
-  if (T32)
-    lvl = (uint32_t)(x1 < (uint32_t)t4) + (uint32_t)(x1 < (uint32_t)t2);
-  else
-    lvl = (uint32_t)((uint64_t)x1 < t4) + (uint32_t)((uint64_t)x1 < t2);
-  return lvl + (x0 < 0x7FFFFFFFu ? 4u : 0u);
+// lane code of one site from its word x (thresholds at most 2^31, so the
+// tests are 32-bit compares)
+__device__ __forceinline__ uint32_t ising_lane_code(uint32_t x, uint32_t t2, uint32_t t4) {
+  const uint32_t y = x & kIsingAcceptMask;
+  return (uint32_t)(y < t4) + (uint32_t)(y < t2) + (x < kIsingProposal1 ? 4u : 0u);
 }
 
 // unlike-neighbour counts of the eight lanes of the segment at stage index c
@@ -236,29 +233,29 @@ __device__ __forceinline__ uint64_t seg_flips(uint64_t e, uint64_t v, uint64_t l
   return (p ^ v) & acc & cmask;
 }
 
-template <typename S, bool T32>
+template <typename S>
 __device__ __forceinline__ int tile_segments_ising8(const TileJob &j, S *stage_s) {
   static_assert(sizeof(S) == 1, "byte lanes");
   int8_t *stage = (int8_t *)stage_s;
   int8_t *dst = (int8_t *)j.dst;
   const int tid = threadIdx.x;
   const RoundKeys rk = round_keys(j.seed, j.key1);
-  const uint64_t t2 = j.thr[2], t4 = j.thr[4];
+  const uint32_t t2 = (uint32_t)j.thr[2], t4 = (uint32_t)j.thr[4];  // at most 2^31
   int changed = 0;
   uint64_t lv[kSegPerThread];
-  // draws: the four x-pairs of each segment
+  // draws: the two Philox blocks of each segment, four sites each
 #pragma unroll
   for (int k = 0; k < kSegPerThread; k++) {
     const int g = tid + k * kTileThreads;
     const int ly = g >> 2, x0 = (g & 3) * 8;
-    const int64_t s = j.base + (int64_t)(j.y0 + ly) * j.L + j.x0 + x0;  // even
+    const int64_t s = j.base + (int64_t)(j.y0 + ly) * j.L + j.x0 + x0;  // a multiple of 8
     uint64_t code = 0;
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const int64_t pr = (s >> 1) + i;
-      U4 w = philox4x32_10_rk(U4{(uint32_t)pr, (uint32_t)(pr >> 32), j.sweep, 0u}, rk);
-      uint32_t c2 = ising_lane_code<T32>(w.x, w.y, t2, t4) | (ising_lane_code<T32>(w.z, w.w, t2, t4) << 8);
-      code |= (uint64_t)c2 << (16 * i);
+    for (int i = 0; i < 2; i++) {
+      U4 w = philox4x32_10_rk(ising_counter((uint64_t)s + 4 * i, j.sweep, 0u), rk);
+      uint32_t c4 = ising_lane_code(w.x, t2, t4) | (ising_lane_code(w.y, t2, t4) << 8) |
+                    (ising_lane_code(w.z, t2, t4) << 16) | (ising_lane_code(w.w, t2, t4) << 24);
+      code |= (uint64_t)c4 << (32 * i);
     }
     lv[k] = code;
   }
@@ -301,11 +298,9 @@ __device__ __forceinline__ int tile_segments_ising8(const TileJob &j, S *stage_s
 // Returns the number of site values changed inside the tile.
 template <int APP, typename S>
 __device__ __forceinline__ int tile_sweep_sq4(const TileJob &j, S *stage) {
-  if constexpr (APP == SPKGPU_ISING && sizeof(S) == 1) {
-    // thr[2] >= thr[4]: one test covers both (uniform across the block)
-    if ((j.thr[2] >> 32) == 0) return tile_segments_ising8<S, true>(j, stage);
-    return tile_segments_ising8<S, false>(j, stage);
-  } else
+  if constexpr (APP == SPKGPU_ISING && sizeof(S) == 1)
+    return tile_segments_ising8<S>(j, stage);
+  else
     return tile_pairs_sq4<APP, S>(j, stage);
 }
 

@@ -17,14 +17,15 @@
 // or 2.  For a lane with value v and neighbour values summing to S (4..8):
 //   unlike neighbours e = S - 4 (v = 1) or 8 - S (v = 2) = (S ^ X) - 3v - 1,
 //   with X = 15 where v = 2 and 0 where v = 1 (15 - S = S ^ 15 for S <= 15).
-// The draws of a site are folded into one code byte
-//   0x9D + lvl - 0x40 p,  lvl = [x1 < thr[4]] + [x1 < thr[2]],  p = [x0 < 2^31-1]
-// (a threshold of 2^32 passes every draw: its test is counted in the start
-// value and the compare is made against 0),
+// The Philox word x of a site (four sites per block) is folded into one code
+// byte
+//   0x9D + lvl - 0x40 p,  lvl = [y < thr[4]] + [y < thr[2]],  p = [x < 2^31],
+//   y = x & 0x7FFFFFFF (the Boltzmann draw; every threshold is at most 2^31,
+//   so the compares are 32-bit and a threshold of 2^31 passes every y),
 // so that s = (S ^ X) + code - 3v = e + lvl + 0x1E + 0x40 (2 - p) per lane:
 // bits 0-5 stay below 0x25, bit 5 is set iff e + lvl >= 2 (the flip, or a
 // proposal equal to the current value, is accepted: e >= 2 means dE <= 0;
-// e = 1 needs x1 < thr[2]; e = 0 needs x1 < thr[4], and thr[4] <= thr[2]),
+// e = 1 needs y < thr[2]; e = 0 needs y < thr[4], and thr[4] <= thr[2]),
 // and bits 6-7 hold the proposed value 2 - p.  The new lane value is the
 // proposal where bit 5 is set in a lane of the phase's colour, else v.  No
 // step carries or borrows across lanes.  At zero temperature thr[] is all
@@ -32,7 +33,8 @@
 //
 // Site values must be 1 or 2 (uploads check the range).  The Philox site
 // counter of a tile is its lattice index (TileJob::base is not used): with
-// x0 and L multiples of 32, every 8-site segment starts at a multiple of 8.
+// x0 and L multiples of 32, every 8-site segment starts at a multiple of 8
+// and takes two whole blocks.
 #pragma once
 
 #include <stdint.h>
@@ -80,16 +82,16 @@ __device__ __forceinline__ uint32_t add_if_below(uint32_t c, uint32_t x, uint32_
   return c;
 }
 
-// adds the code of a site with draws (x0, x1) to the byte at bit SH of c,
-// which starts at 0x9D plus the number of threshold tests that always pass
-// (thr >= 2^32); t2c and t4c are the thresholds below 2^32, else 0
+// adds the code of a site with Philox word x to the byte at bit SH of c,
+// which starts at 0x9D; t2 and t4 are thr[2] and thr[4] (at most 2^31)
 template <int SH>
-__device__ __forceinline__ uint32_t add_lane_code(uint32_t c, uint32_t x0, uint32_t x1, uint32_t t2c, uint32_t t4c) {
-  asm("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %1, 0x7FFFFFFF;\n\t@q add.u32 %0, %0, %2;\n\t}"
+__device__ __forceinline__ uint32_t add_lane_code(uint32_t c, uint32_t x, uint32_t t2, uint32_t t4) {
+  asm("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %1, 0x80000000;\n\t@q add.u32 %0, %0, %2;\n\t}"
       : "+r"(c)
-      : "r"(x0), "n"(0u - (0x40u << SH)));
-  c = add_if_below<1u << SH>(c, x1, t4c);
-  return add_if_below<1u << SH>(c, x1, t2c);
+      : "r"(x), "n"(0u - (0x40u << SH)));
+  const uint32_t y = x & kIsingAcceptMask;
+  c = add_if_below<1u << SH>(c, y, t4);
+  return add_if_below<1u << SH>(c, y, t2);
 }
 
 // ring site k (0..63) of the tile, as in ring_site: rows -1 and 32, then
@@ -123,9 +125,7 @@ struct WarpDraws {
 template <int M0, int M1, bool RING>
 __device__ __forceinline__ void warp_draws(const TileJob &j, int lane, WarpDraws &d) {
   const RoundKeys rk = round_keys(j.seed, j.key1);
-  const bool big2 = (j.t2 >> 32) != 0, big4 = (j.t4 >> 32) != 0;
-  const uint32_t t2c = big2 ? 0u : (uint32_t)j.t2, t4c = big4 ? 0u : (uint32_t)j.t4;
-  const uint32_t c0 = 0x9D9D9D9Du + 0x01010101u * ((big2 ? 1u : 0u) + (big4 ? 1u : 0u));
+  const uint32_t t2 = (uint32_t)j.t2, t4 = (uint32_t)j.t4;  // at most 2^31
   // the ring first: its codes then stay live in two registers only
 #pragma unroll
   for (int r = 0; r < (RING ? 2 : 0); r++) {
@@ -135,23 +135,20 @@ __device__ __forceinline__ void warp_draws(const TileJob &j, int lane, WarpDraws
     gy = gy < 0 ? gy + j.Ly : (gy >= j.Ly ? gy - j.Ly : gy);
     gx = gx < 0 ? gx + j.L : (gx >= j.L ? gx - j.L : gx);
     const int64_t s = (int64_t)gy * j.L + gx;
-    const U4 w = philox4x32_10_rk(U4{(uint32_t)(s >> 1), (uint32_t)(s >> 33), j.sweep, 0u}, rk);
-    const bool odd = s & 1;
-    d.ring[r] = add_lane_code<0>(c0 & 0xFFu, odd ? w.z : w.x, odd ? w.w : w.y, t2c, t4c);
+    const U4 w = philox4x32_10_rk(ising_counter((uint64_t)s, j.sweep, 0u), rk);
+    d.ring[r] = add_lane_code<0>(0x9Du, block_word(w, (int)(s & 3)), t2, t4);
   }
 #pragma unroll
   for (int m = M0; m < M1; m++) {
     const int ly = (lane >> 2) + 8 * m;
-    const int64_t s = (int64_t)(j.y0 + ly) * j.L + j.x0 + 8 * (lane & 3);
-    const uint32_t plo = (uint32_t)(s >> 1), phi = (uint32_t)(s >> 33);  // plo % 4 == 0
+    const int64_t s = (int64_t)(j.y0 + ly) * j.L + j.x0 + 8 * (lane & 3);  // a multiple of 8
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-      const U4 w0 = philox4x32_10_rk(U4{plo + (uint32_t)(2 * h), phi, j.sweep, 0u}, rk);
-      uint32_t c = add_lane_code<0>(c0, w0.x, w0.y, t2c, t4c);
-      c = add_lane_code<8>(c, w0.z, w0.w, t2c, t4c);
-      const U4 w1 = philox4x32_10_rk(U4{plo + (uint32_t)(2 * h + 1), phi, j.sweep, 0u}, rk);
-      c = add_lane_code<16>(c, w1.x, w1.y, t2c, t4c);
-      d.code[2 * m + h] = add_lane_code<24>(c, w1.z, w1.w, t2c, t4c);
+      const U4 w = philox4x32_10_rk(ising_counter((uint64_t)s + 4 * h, j.sweep, 0u), rk);
+      uint32_t c = add_lane_code<0>(0x9D9D9D9Du, w.x, t2, t4);
+      c = add_lane_code<8>(c, w.y, t2, t4);
+      c = add_lane_code<16>(c, w.z, t2, t4);
+      d.code[2 * m + h] = add_lane_code<24>(c, w.w, t2, t4);
     }
   }
 }
