@@ -200,3 +200,27 @@ def test_diagnostics_match_unmodified_reference_log(ref_fixtures, k):
             naccept, nattempt, done = naccept + na, nattempt + nt, done + sweeps
         assert [int(row[1]), int(row[2])] == [naccept, nattempt - naccept]
         assert diag_tokens(cfg, spin, sp["diags"]) == row[5:], fx["case"]["name"]
+
+
+def test_ising_sweep_takes_one_word_per_site():
+    """At kT = 1e30 every Ising move is accepted (floor(exp(-dE/T) 2^31) = 2^31), so after one sweep site s
+    holds the proposal of its own word: word s&3 of the block with counter (s>>2, s>>34, sweep, pass), value 1
+    iff the word is below 2^31.  Rows of 6 sites make blocks straddle rows."""
+    seed = 4242
+    c = oracle.make_cfg("sq/4n", 6, 4, 1, "ising", 2, 1e30, seed=seed)
+    spin = np.full(24, 2, dtype=np.int32)
+    oracle.color_sweeps(c, spin, 7, 1)
+    want = [1 if oracle.philox([s >> 2, 0, 7, 0], [seed, 0])[s & 3] < 2**31 else 2 for s in range(24)]
+    assert spin.tolist() == want
+
+
+def test_potts_sweep_takes_two_words_per_site():
+    """The Potts-family apps keep two words per site: at kT = 1e30 site s proposes
+    (int)(Q (x+1) 2^-32) + 1 from word 2(s&1) of the block with counter (s>>1, s>>33, sweep, pass)."""
+    seed, q = 99, 5
+    c = oracle.make_cfg("sq/4n", 6, 4, 1, "potts", q, 1e30, seed=seed)
+    spin = np.full(24, 1, dtype=np.int32)
+    oracle.color_sweeps(c, spin, 3, 1)
+    want = [min(q, (q * (oracle.philox([s >> 1, 0, 3, 0], [seed, 0])[2 * (s & 1)] + 1)) // 2**32 + 1)
+            for s in range(24)]
+    assert spin.tolist() == want
