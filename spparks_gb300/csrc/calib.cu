@@ -1,9 +1,10 @@
 // Calibration of the integer-issue ceiling of the sweep kernels: how many
 // Philox4x32-10 blocks per second this device computes with the sweeps' own
 // Philox code (hoisted round keys, four independent blocks per thread in
-// flight), with nothing else in the loop.  Every sweep of the Philox draw
-// contract spends one block per x-pair of sites, so twice this rate bounds
-// any sweep from above.  No counterpart in the reference.
+// flight), with nothing else in the loop.  An Ising sweep of the Philox draw
+// contract spends one block per four sites and the other apps one per x-pair,
+// so four (ising) or two times this rate bounds a sweep from above.  No
+// counterpart in the reference.
 
 #include <cuda_runtime.h>
 

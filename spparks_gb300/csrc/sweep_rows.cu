@@ -6,7 +6,8 @@
 // the same row.  A CTA therefore sweeps whole x-rows: it stages the row and
 // its 8 (3d) or 2 (2d) neighbouring rows in shared memory, updates the even
 // sites, synchronises, then the odd sites - each thread owning one x-pair
-// whose Philox block serves both of its sites.  Rows of other parities are
+// whose Philox block serves both of its sites (for ising the block holds the
+// words of four sites; the pair's two are used).  Rows of other parities are
 // not written during the launch, so the order equals the reference's colour
 // order (src/app_lattice.cpp:672-680).
 //
