@@ -27,9 +27,14 @@
 // proposal equal to the current value, is accepted: e >= 2 means dE <= 0;
 // e = 1 needs y < thr[2]; e = 0 needs y < thr[4], and thr[4] <= thr[2]),
 // and bits 6-7 hold the proposed value 2 - p.  The new lane value is the
-// proposal where bit 5 is set in a lane of the phase's colour, else v.  No
-// step carries or borrows across lanes.  At zero temperature thr[] is all
-// zero, so lvl = 0 and only e >= 2 is accepted.
+// proposal where bit 5 is set, else v.  No step carries or borrows across
+// lanes.  At zero temperature thr[] is all zero, so lvl = 0 and only e >= 2
+// is accepted.
+//
+// A colour phase takes the four sites of the phase's colour out of each
+// 8-site segment (every other byte: the colours alternate along x) into one
+// word with __byte_perm, so the lane rule runs once per four sites of the
+// phase, and puts the new values back in x order.
 //
 // Site values must be 1 or 2 (uploads check the range).  The Philox site
 // counter of a tile is its lattice index (TileJob::base is not used): with
@@ -113,9 +118,18 @@ __device__ __forceinline__ void warp_ring_pos(int k, int &rlx, int &rly) {
   }
 }
 
+// __byte_perm selectors taking the sites of x parity 0 (x0, x0+2, x0+4, x0+6)
+// or parity 1 out of a segment held as (sites x0..x0+3, sites x0+4..x0+7)
+constexpr uint32_t kSelEven = 0x6420u, kSelOdd = 0x7531u;
+
+// selector of the x parity of the colour-1 sites of this lane's rows (all its
+// rows have the parity of row lane>>2)
+__device__ __forceinline__ uint32_t colour1_selector(int lane) { return kSelEven + 0x1111u * ((lane >> 2) & 1); }
+
 // the codes of a lane's sites: segment m (row (lane>>2) + 8m, columns
-// 8(lane&3) .. +7) in code[2m] (lanes 0-3) and code[2m+1] (lanes 4-7); the
-// lane's ring sites k = lane and lane+32 in the low bytes of ring[]
+// 8(lane&3) .. +7) as its four colour-1 sites in code[2m] and its four
+// colour-2 sites in code[2m+1], in x order; the lane's ring sites k = lane
+// and lane+32 in the low bytes of ring[]
 struct WarpDraws {
   uint32_t code[2 * kWSegPerLane];
   uint32_t ring[2];
@@ -138,45 +152,74 @@ __device__ __forceinline__ void warp_draws(const TileJob &j, int lane, WarpDraws
     const U4 w = philox4x32_10_rk(ising_counter((uint64_t)s, j.sweep, 0u), rk);
     d.ring[r] = add_lane_code<0>(0x9Du, block_word(w, (int)(s & 3)), t2, t4);
   }
+  const uint32_t sel1 = colour1_selector(lane);
 #pragma unroll
   for (int m = M0; m < M1; m++) {
     const int ly = (lane >> 2) + 8 * m;
     const int64_t s = (int64_t)(j.y0 + ly) * j.L + j.x0 + 8 * (lane & 3);  // a multiple of 8
+    uint32_t cw[2];  // codes of sites x0..x0+3 and x0+4..x0+7
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       const U4 w = philox4x32_10_rk(ising_counter((uint64_t)s + 4 * h, j.sweep, 0u), rk);
       uint32_t c = add_lane_code<0>(0x9D9D9D9Du, w.x, t2, t4);
       c = add_lane_code<8>(c, w.y, t2, t4);
       c = add_lane_code<16>(c, w.z, t2, t4);
-      d.code[2 * m + h] = add_lane_code<24>(c, w.w, t2, t4);
+      cw[h] = add_lane_code<24>(c, w.w, t2, t4);
     }
+    d.code[2 * m] = __byte_perm(cw[0], cw[1], sel1);
+    d.code[2 * m + 1] = __byte_perm(cw[0], cw[1], sel1 ^ 0x1111u);
   }
 }
 
-// new values of four lanes v with neighbour words l, u, dn, r and codes
-// `code`; cm = 0x20 in the lanes of the phase's colour
-__device__ __forceinline__ uint32_t warp_lanes(uint32_t v, uint32_t l, uint32_t u, uint32_t dn, uint32_t r,
-                                               uint32_t code, uint32_t cm) {
-  const uint32_t sum = l + u + dn + r;
+// new values of four lanes v, all of the phase's colour, with neighbour
+// values summing to `sum` per lane and codes `code`
+__device__ __forceinline__ uint32_t warp_lanes(uint32_t v, uint32_t sum, uint32_t code) {
   const uint32_t x = v * 15u - 0x0F0F0F0Fu;
   const uint32_t s = (sum ^ x) + (code - 3u * v);
-  const uint32_t am = (s & cm) * 6u;  // bits 6-7 of the accepted lanes
+  const uint32_t am = (s & 0x20202020u) * 6u;  // bits 6-7 of the accepted lanes
   return ((s & am) | ((v << 6) & ~am)) >> 6;
 }
 
-// one colour phase of segment m: reads the stage, returns the new segment
-__device__ __forceinline__ uint2 warp_segment(const int8_t *stage, int c, const WarpDraws &d, int m, uint32_t cm,
-                                              uint2 &v) {
-  v = *(const uint2 *)(stage + c);
+// __byte_perm selectors and offsets of one colour phase for a lane whose
+// active sites (the phase's colour) have x parity P
+struct PhaseSel {
+  uint32_t act, other;  // the active / other x parity of a segment
+  uint32_t side;        // the active sites' neighbours across the segment edge
+  int side_off;         // stage offset of the word holding that edge site
+  uint32_t lo, hi;      // interleave (new active, other) back into x order
+};
+
+__device__ __forceinline__ PhaseSel phase_sel(uint32_t act) {
+  const bool odd = act == kSelOdd;
+  PhaseSel p;
+  p.act = act;
+  p.other = act ^ 0x1111u;
+  // parity 0: left neighbours [x0-1, x0+1, x0+3, x0+5] from the word ending
+  // at x0-1 and the odd sites; parity 1: right neighbours [x0+2 .. x0+8]
+  p.side = odd ? 0x4321u : 0x2107u;
+  p.side_off = odd ? 8 : -4;
+  p.lo = odd ? 0x1504u : 0x5140u;
+  p.hi = odd ? 0x3726u : 0x7362u;
+  return p;
+}
+
+// one colour phase of a segment at stage index c: the four active sites are
+// gathered into one word (their left and right neighbours are the other
+// four sites and one edge site, their up and down neighbours the same x
+// parity of the rows above and below), updated, and put back in x order;
+// *diff gets the changed lanes (3 in each changed byte)
+__device__ __forceinline__ uint2 warp_segment(const int8_t *stage, int c, uint32_t code, const PhaseSel &p,
+                                              uint32_t *diff) {
+  const uint2 v = *(const uint2 *)(stage + c);
   const uint2 up = *(const uint2 *)(stage + c - kWStageX);
   const uint2 dn = *(const uint2 *)(stage + c + kWStageX);
-  const uint32_t lw = *(const uint32_t *)(stage + c - 4);  // top byte: site x0-1
-  const uint32_t rw = *(const uint32_t *)(stage + c + 8);  // low byte: site x0+8
-  uint2 n;
-  n.x = warp_lanes(v.x, __funnelshift_l(lw, v.x, 8), up.x, dn.x, __funnelshift_r(v.x, v.y, 8), d.code[2 * m], cm);
-  n.y = warp_lanes(v.y, __funnelshift_l(v.x, v.y, 8), up.y, dn.y, __funnelshift_r(v.y, rw, 8), d.code[2 * m + 1],
-                   cm);
-  return n;
+  const uint32_t edge = *(const uint32_t *)(stage + c + p.side_off);
+  const uint32_t a = __byte_perm(v.x, v.y, p.act), b = __byte_perm(v.x, v.y, p.other);
+  const uint32_t sum = b + __byte_perm(b, edge, p.side) + __byte_perm(up.x, up.y, p.act) +
+                       __byte_perm(dn.x, dn.y, p.act);
+  const uint32_t an = warp_lanes(a, sum, code);
+  *diff = a ^ an;
+  return make_uint2(__byte_perm(an, b, p.lo), __byte_perm(an, b, p.hi));
 }
 
 // bit 7 of each byte lane set where the lane of d is non-zero
@@ -233,16 +276,17 @@ __device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *st
                                                     unsigned int *bonds) {
   int8_t *dst = (int8_t *)j.dst;
   const int x0 = 8 * (lane & 3);
-  // colour-1 lanes have the parity of the row; rows of a lane share a parity
-  const uint32_t cm1 = ((lane >> 2) & 1) ? 0x20002000u : 0x00200020u;
-  const uint32_t cm2 = cm1 ^ 0x20202020u;
+  // colour-1 sites have the x parity of the row; rows of a lane share a parity
+  const PhaseSel p1 = phase_sel(colour1_selector(lane));
   uint32_t cnt = 0;  // 3 per changed site, per byte lane
 #pragma unroll
   for (int m = 0; m < kWSegPerLane; m++) {
     const int c = wstage_at(x0, (lane >> 2) + 8 * m);
-    uint2 v;
-    const uint2 n = warp_segment(stage, c, d, m, cm1, v);
-    cnt += (v.x ^ n.x) + (v.y ^ n.y);
+    uint32_t diff;
+    const uint2 n = warp_segment(stage, c, d.code[2 * m], p1, &diff);
+    cnt += diff;
+    // only colour-1 sites change; readers of this word in this phase use only
+    // its colour-2 sites, which are written back unchanged
     *(uint2 *)(stage + c) = n;
   }
 #pragma unroll
@@ -258,13 +302,14 @@ __device__ __forceinline__ unsigned int warp_phases(const TileJob &j, int8_t *st
     if ((s & 0x20u) && (s >> 6) != own) stage[c] = (int8_t)(s >> 6);
   }
   __syncwarp();
+  const PhaseSel p2 = phase_sel(p1.other);
 #pragma unroll
   for (int m = 0; m < kWSegPerLane; m++) {
     const int ly = (lane >> 2) + 8 * m;
-    uint2 v;
     const int c = wstage_at(x0, ly);
-    const uint2 n = warp_segment(stage, c, d, m, cm2, v);
-    cnt += (v.x ^ n.x) + (v.y ^ n.y);
+    uint32_t diff;
+    const uint2 n = warp_segment(stage, c, d.code[2 * m + 1], p2, &diff);
+    cnt += diff;
     *(uint2 *)(dst + (int64_t)(j.y0 + ly) * j.L + j.x0 + x0) = n;
     // the colour-2 lanes are final; readers of this word in this phase use
     // only its colour-1 lanes, which do not change
