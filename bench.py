@@ -434,6 +434,23 @@ def kernel_case(name):
         lat.init_spins(1, 2)
         lat.sweep(2)
         print("packed", lat.stats())
+    elif name == "rates":  # site-updates/s of the single-lattice sweeps, CUDA events on each lattice's stream
+        cases = [
+            ("sq/4n 128^2 ising int32, 100 sweeps", ("sq/4n", 128, 128, 1, "ising", 2, 4), 2.269, 100),
+            ("sc/6n 1536^3 ising bit-packed", ("sc/6n", 1536, 1536, 1536, "ising", 2, -1), 4.5115, 3),
+            ("sc/6n 1536^3 ising int8", ("sc/6n", 1536, 1536, 1536, "ising", 2, 1), 4.5115, 2),
+            ("sq/4n 12288^2 ising int8", ("sq/4n", 12288, 12288, 1, "ising", 2, 1), 2.269, 20),
+            ("sq/4n 12288^2 ising int16", ("sq/4n", 12288, 12288, 1, "ising", 2, 2), 2.269, 10),
+            ("sq/4n 12288^2 potts Q=2 int8", ("sq/4n", 12288, 12288, 1, "potts", 2, 1), 1.0, 10),
+        ]
+        for label, (lt, nx, ny, nz, app, q, sb), temp, nsw in cases:
+            lat = sg.Lattice(lt, nx, ny, nz, app, q, spin_bytes=sb, seed=56789)
+            lat.set_temperature(temp)
+            lat.init_spins(1, q)
+            lat.timed_sweeps(1)
+            ms = lat.timed_sweeps(nsw)
+            print(f"{label}: {ms / nsw:.4f} ms per sweep, {lat.n * nsw / (ms * 1e-3):.3e} site-updates/s", flush=True)
+            lat.close()
     elif name == "kmc":  # tree KMC Potts Q=50 sq/8n 1024^2, 32x32 processor grid, 4 sectors
         lat = sg.Lattice("sq/8n", 1024, 1024, 1, "potts", 50, spin_bytes=4, nsector=4, procs=(32, 32, 1), seed=5)
         lat.set_temperature(1.0)
@@ -451,7 +468,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--kernel-case", choices=["ensemble", "fused", "rows", "packed", "kmc"],
+    ap.add_argument("--kernel-case", choices=["ensemble", "fused", "rows", "packed", "kmc", "rates"],
                     help="run one small profiling workload instead of the benchmark")
     args = ap.parse_args()
     if args.kernel_case:
