@@ -6,7 +6,9 @@ Workload (the configuration the headline metric is quoted on): the batched
 spins uniform from the seed, replica exchange between neighbouring
 temperatures (of equal-L replicas) every 10 sweeps, 2000 sweeps in all.
 One step = 10 sweeps of every replica plus one exchange round = one replay of
-a captured CUDA graph holding one persistent cooperative launch.
+a captured CUDA graph in the execution form the ensemble's autotuner keeps
+(on GB300: 10 warp-tile sweep launches, the last also counting the unlike
+bonds, then the exchange round).
 
   value      site-updates/s with the spins resident in HBM (CUDA events)
   e2e        the same through the C ABI with pinned host buffers: each step
@@ -16,12 +18,12 @@ a captured CUDA graph holding one persistent cooperative launch.
              per-colour phase kernel (a bounded sample, extrapolated)
   roofline   algorithmic HBM bytes (2 bytes per int8 site-update) / kernel
              time, against the measured copy bandwidth
-  cpu_baseline  the oracle port (C restatement of the reference's colour
-             sweep) on the host cores over a bounded sample
+  cpu_baseline  the reference's own colour sweep (SPPARKS built from its
+             sources on this host) on one core over a bounded sample; the
+             oracle port where the reference does not build
 
-`--impl reference` times that CPU implementation alone on all host cores
-(the reference sources are not present on the GPU host; its compiled x86
-build cannot run there) and prints the same JSON line.
+`--impl reference` times that CPU implementation alone on all host cores and
+prints the same JSON line.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -86,22 +88,54 @@ def profile_traffic(name):
     return None, None
 
 
+def gpu_identity(device):
+    """The benchmarked GPU as nvidia-smi names it: its UUID (or PCI bus id),
+    taken from the CUDA device, so that CUDA_VISIBLE_DEVICES remapping cannot
+    point the clock samples at another GPU.  Returns (id, how it was found)."""
+    import torch
+
+    props = torch.cuda.get_device_properties(device)
+    cands = []
+    uuid = getattr(props, "uuid", None)
+    if uuid is not None:
+        u = str(uuid)
+        cands.append((u if u.startswith("GPU-") else "GPU-" + u, "uuid"))
+    bus = getattr(props, "pci_bus_id", None)
+    if bus is not None:
+        cands.append((f"{getattr(props, 'pci_domain_id', 0):08x}:{bus:02x}:{getattr(props, 'pci_device_id', 0):02x}.0",
+                      "pci bus id"))
+    for ident, how in cands:
+        try:
+            r = subprocess.run(["nvidia-smi", f"--id={ident}", "--query-gpu=uuid", "--format=csv,noheader"],
+                               capture_output=True, text=True, timeout=20)
+            if r.returncode == 0 and r.stdout.strip():
+                return ident, how
+        except Exception:
+            pass
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    parts = [x.strip() for x in vis.split(",") if x.strip()]
+    if parts and device < len(parts):
+        return parts[device], "CUDA_VISIBLE_DEVICES entry"
+    return str(device), "CUDA ordinal (no remapping in effect)"
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons during the timed region, on the
+    benchmarked GPU named by identity (gpu_identity)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
-        self.index = index
+    def __init__(self, device=0):
+        self.ident, self.ident_how = gpu_identity(device)
         self.proc = None
         self.path = Path(tempfile.gettempdir()) / f"spk_bench_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:
             self.f = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.ident}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
@@ -109,7 +143,7 @@ class ClockSampler:
 
     def stop(self):
         if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "gpu": self.ident}
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -135,14 +169,84 @@ class ClockSampler:
         except OSError:
             pass
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "gpu": self.ident, "gpu_id": self.ident_how}
 
 
 # ---------------------------------------------------------------------------
-# CPU implementation (oracle port) - reference arm and cpu_baseline
+# CPU implementations - reference arm and cpu_baseline
+#
+# The reference itself (kind "reference"): SPPARKS built from its own sources
+# by oracle/ref/Makefile, natively on this host (from the staged copy of its
+# sources where the reference tree is absent), driven through its library
+# interface by oracle/_ref/runner_plain.  Each replica is one reference run:
+# `app_style ising`, `lattice sq/4n`, `sweep color`, its temperature, its
+# own seed, and `run 2` = 4 sweeps (dt_sweep = 1/2 for ising,
+# src/app_ising.cpp:41); the runner times each `run` with a monotonic clock.
+# The oracle port (kind "port", the C restatement) is the fallback when the
+# reference did not build here.
 
 
-def _cpu_worker(args):
+def sample_replicas(nrep, procs, offset=0):
+    """`nrep` random replicas of the workload's distribution, assigned to
+    `procs` workers longest-first so that every worker holds about the same
+    number of sites."""
+    L, T = ensemble_config()
+    rng = np.random.default_rng(7 + offset)
+    pick = rng.choice(len(L), size=min(nrep, len(L)), replace=False)
+    reps = sorted([(int(r), int(L[r]), float(T[r])) for r in pick], key=lambda x: -x[1])
+    chunks, load = [[] for _ in range(procs)], [0] * procs
+    for rep in reps:
+        k = load.index(min(load))
+        chunks[k].append(rep)
+        load[k] += rep[1] ** 2
+    return chunks
+
+
+def _reference_script(reps, sweeps, warmup, steps, seed):
+    lines = []
+    for r, L, T in reps:
+        lines += [f"seed {seed + r}", "app_style ising", "dimension 2", "lattice sq/4n 1.0",
+                  f"region box block 0 {L} 0 {L} -0.5 0.5", "create_box box", "create_sites box",
+                  "set site range 1 2", "sweep color", f"temperature {T!r}"]
+        lines += [f"run {sweeps / 2!r}"] * warmup
+        lines += [f"#! timed {k} run {sweeps / 2!r}" for k in range(steps)]
+        lines.append("clear")
+    return "\n".join(lines) + "\n"
+
+
+def reference_cpu_rate(chunks, sweeps, warmup, steps, binary):
+    """The reference's own colour sweep, one runner process per chunk, all
+    at once.  A step is every replica of every chunk swept `sweeps` times;
+    its time is the slowest worker's summed `run` time for that step.
+    Returns (site-updates/s, updates, per-step seconds)."""
+    procs, files = [], []
+    tmpdir = Path(tempfile.mkdtemp(prefix="spk_ref_"))
+    for w, reps in enumerate(chunks):
+        f = tmpdir / f"in.{w}"
+        f.write_text(_reference_script(reps, sweeps, warmup, steps, SEED))
+        files.append(f)
+        procs.append(subprocess.Popen([str(binary), str(f)], stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                                      text=True, cwd=str(tmpdir)))
+    per_worker = []
+    for pr in procs:
+        out, err = pr.communicate()
+        if pr.returncode != 0:
+            raise RuntimeError(f"reference runner failed ({pr.returncode}): {err[-400:]}")
+        t = [0.0] * steps
+        for line in out.splitlines():
+            p = line.split()
+            if len(p) == 3 and p[0] == "timed":
+                t[int(p[1])] += float(p[2])
+        per_worker.append(t)
+    for f in files:
+        f.unlink()
+    tmpdir.rmdir()
+    step_s = [max(t[k] for t in per_worker) for k in range(steps)]
+    updates = sum(L * L for reps in chunks for _, L, _ in reps) * sweeps * steps
+    return updates / sum(step_s), updates, step_s
+
+
+def _port_worker(args):
     reps, sweeps, seed = args
     import oracle
 
@@ -156,66 +260,99 @@ def _cpu_worker(args):
     return done, time.perf_counter() - t0
 
 
-def cpu_rate(sample_replicas=24, sweeps=4, procs=1, pool=None, offset=0):
-    """Site-updates/s of the oracle's colour sweep on a sample of replicas
-    (wall time of the sample; `pool` is a persistent spawn pool of `procs`)."""
-    L, T = ensemble_config()
-    rng = np.random.default_rng(7 + offset)
-    pick = rng.choice(len(L), size=min(sample_replicas, len(L)), replace=False)
-    reps = sorted([(int(r), int(L[r]), float(T[r])) for r in pick], key=lambda x: -x[1])
-    # longest-processing-time assignment: equal site counts per process
-    chunks, load = [[] for _ in range(procs)], [0] * procs
-    for rep in reps:
-        k = load.index(min(load))
-        chunks[k].append(rep)
-        load[k] += rep[1] ** 2
+def port_cpu_rate(chunks, sweeps, pool=None):
+    """Site-updates/s of the oracle port's colour sweep over `chunks` (wall
+    time of the sample; `pool` is a persistent spawn pool of len(chunks))."""
     t0 = time.perf_counter()
     if pool is None:
-        results = [_cpu_worker((chunks[0], sweeps, SEED))]
+        results = [_port_worker((c, sweeps, SEED)) for c in chunks]
     else:
-        results = pool.map(_cpu_worker, [(c, sweeps, SEED) for c in chunks])
+        results = pool.map(_port_worker, [(c, sweeps, SEED) for c in chunks])
     wall = time.perf_counter() - t0
     updates = sum(r[0] for r in results)
     return updates / wall, updates, wall
 
 
+def reference_binary():
+    """runner_plain built natively here, or (None, why not)."""
+    import oracle
+
+    try:
+        oracle.build_reference()
+    except Exception as e:  # a failed native build falls back to the port
+        return None, f"reference build failed: {str(e)[-200:]}"
+    b = oracle.reference_binary("runner_plain")
+    return (b, None) if b else (None, "reference sources absent on this host")
+
+
 def run_reference(args):
-    """The reference's CPU colour sweep (the oracle port: the reference's x86
-    build cannot run on the GPU host) on every host core: one spawned process
-    per core, each step 4 replicas per process (equal site counts) x 4 sweeps."""
+    """The reference's CPU colour sweep on every host core: one reference
+    runner per core, each step 4 random replicas per core (about equal sites
+    per core) x 4 sweeps.  Falls back to the oracle port, labelled, when the
+    reference cannot be built here."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import multiprocessing as mp
-
-    import oracle
-
-    oracle.build()
     procs = os.cpu_count() or 1
     sweeps = 4
-    with mp.get_context("spawn").Pool(procs) as pool:
-        for w in range(args.warmup):
-            cpu_rate(sample_replicas=procs, sweeps=1, procs=procs, pool=pool, offset=1000 + w)
-        times, ups = [], 0
-        for k in range(args.steps):
-            r, u, w = cpu_rate(sample_replicas=4 * procs, sweeps=sweeps, procs=procs, pool=pool, offset=k)
-            times.append(w)
-            ups += u
-    value = ups / sum(times)
+    binary, why = reference_binary()
+    if binary:
+        chunks = sample_replicas(4 * procs, procs)
+        value, ups, step_s = reference_cpu_rate(chunks, sweeps, args.warmup, args.steps, binary)
+        kind = "reference"
+        sample = (f"{4 * procs} random replicas x {sweeps} sweeps per step, one reference runner per core: "
+                  "SPPARKS built from its own sources on this host, app_style ising, sweep color, stock RandomPark")
+    else:
+        import multiprocessing as mp
+
+        import oracle
+
+        oracle.build()
+        with mp.get_context("spawn").Pool(procs) as pool:
+            for w in range(args.warmup):
+                port_cpu_rate(sample_replicas(procs, procs, 1000 + w), 1, pool)
+            step_s, ups = [], 0
+            for k in range(args.steps):
+                _, u, wall = port_cpu_rate(sample_replicas(4 * procs, procs, k), sweeps, pool)
+                step_s.append(wall)
+                ups += u
+        value = ups / sum(step_s)
+        kind = "port"
+        sample = (f"{4 * procs} replicas x {sweeps} sweeps per step, oracle C restatement of "
+                  f"AppIsing::site_event_rejection + colour sweep, one process per core ({why})")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(step_s), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "impl": "reference",
         "config": {"workload": "batched 2D Ising ensemble, 512 sq/4n replicas L in [64,1024], kT in [1.5,3.5], "
-                               "exchange every 10 sweeps", "step": f"{sweeps} sweeps of {4 * procs} random replicas, equal sites per core",
+                               "exchange every 10 sweeps", "step": f"{sweeps} sweeps of {4 * procs} random replicas, "
+                                                                   "about equal sites per core",
                    "threads": procs},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": f"{4 * procs} replicas x {sweeps} sweeps per step, oracle C restatement of "
-                                   "AppIsing::site_event_rejection + colour sweep, one process per core"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_leg():
+    """About 10 s of one host core on a bounded sample of the workload: the
+    reference itself where it builds here, else the oracle port."""
+    binary, why = reference_binary()
+    if binary:
+        chunks = sample_replicas(24, 1, 3)
+        sweeps = 48  # about 1.6e8 site-updates: 8 s at the 2e7/s of one Grace core
+        r, u, step_s = reference_cpu_rate(chunks, sweeps, 0, 1, binary)
+        return {"value": r, "unit": UNIT, "cores": 1, "kind": "reference",
+                "sample": f"24 random replicas x {sweeps} sweeps ({u:.3g} site-updates, {sum(step_s):.1f} s), "
+                          "SPPARKS built from its own sources on this host (app_style ising, sweep color), 1 core"}
+    import oracle
+
+    oracle.build()
+    r, u, w = port_cpu_rate(sample_replicas(48, 1, 0), 40)
+    return {"value": r, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"48 random replicas x 40 sweeps ({u:.3g} site-updates, {w:.1f} s), oracle C "
+                      f"restatement of the reference colour sweep, 1 thread ({why})"}
 
 
 # ---------------------------------------------------------------------------
@@ -354,20 +491,12 @@ def run_ours(args):
     kernel_ms = kern_ms / max(kern_launches, 1)
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     traffic, traffic_src = profile_traffic(kname)
-    # the draw-side ceiling: one Philox4x32-10 block per x-pair of sites
+    # the draw-side ceiling: one Philox4x32-10 block per four Ising sites
     philox_bps = sg.philox_rate(device, 1024)
 
     if rank != 0:
         return
-    cpu = None
-    if not args.no_cpu:
-        import oracle
-
-        oracle.build()
-        r1, u1, w1 = cpu_rate(sample_replicas=48, sweeps=40, procs=1)  # about 10 s of one core
-        cpu = {"value": r1, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"48 random replicas x 40 sweeps ({u1:.3g} site-updates, {w1:.1f} s), oracle C "
-                         "restatement of the reference colour sweep, 1 thread"}
+    cpu = None if args.no_cpu else cpu_baseline_leg()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

@@ -203,10 +203,13 @@ int spkgpu_philox_rate(int32_t device, int32_t iters, double *blocks_per_s);
    SPKGPU_ERR_TOO_LARGE.  The array is shared by all calls and keeps the last
    call's contents, so calls whose GPU work overlaps race: serialise them.
    The first call on a device looks up the array's device address
-   (cudaGetSymbolAddress) and should precede any stream capture.  Work goes
-   on `stream` (a cudaStream_t, NULL = default stream); if naccept is not
+   (cudaGetSymbolAddress) and should precede any stream capture; it is
+   looked up again when the device's context changes (cudaDeviceReset).  Work
+   goes on `stream` (a cudaStream_t, NULL = default stream); if naccept is not
    NULL the call waits for the stream and stores the number of changed site
-   values there, otherwise it returns without waiting.  It allocates nothing. */
+   values there, otherwise it returns without waiting.  Inside a stream
+   capture naccept must be NULL (SPKGPU_ERR_ARG otherwise, with nothing
+   enqueued).  It allocates nothing. */
 #define SPKGPU_NOALLOC_MAX_BYTES (4u << 20)
 int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int32_t spin_bytes, int32_t app,
                              int32_t nspins, double temperature, uint32_t seed, int64_t sweep0,

@@ -37,14 +37,34 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
-def build_reference(jobs: int = 8) -> bool:
-    """Build the reference (and its Philox-shim variant) into ``oracle/_ref``
-    when the reference sources are present; returns False when they are not."""
+REF_OUT = HERE / "_ref"
+REF_STAGE = REF_OUT / "src"
+
+
+def build_reference(jobs: int = 0) -> bool:
+    """Build the reference (and its Philox-shim variant) into ``oracle/_ref``.
+
+    Where the reference tree exists, its sources are also staged into
+    ``oracle/_ref/src`` (git-ignored); where it does not (the GPU host), the
+    same recipe builds from that staged copy, natively for the host CPU.
+    Returns False when neither is present."""
+    jobs = jobs or max(2, os.cpu_count() or 2)
     ref = os.environ.get("SPK_REFERENCE_SRC", "/root/reference/src")
-    if not Path(ref, "app_lattice.cpp").exists():
+    make = ["make", "-s", "-C", str(HERE / "ref"), f"-j{jobs}"]
+    if Path(ref, "app_lattice.cpp").exists():
+        subprocess.check_call(make + ["stage", f"REF={ref}"])
+    elif Path(REF_STAGE, "app_lattice.cpp").exists():
+        ref = str(REF_STAGE)
+    else:
         return False
-    subprocess.check_call(["make", "-s", "-C", str(HERE / "ref"), f"-j{jobs}", f"REF={ref}"])
+    subprocess.check_call(make + [f"REF={ref}"])
     return True
+
+
+def reference_binary(name: str = "runner_plain"):
+    """Path of a reference binary built by build_reference, or None."""
+    p = REF_OUT / name
+    return p if p.exists() and os.access(p, os.X_OK) else None
 
 
 class Cfg(ctypes.Structure):

@@ -10,10 +10,12 @@
      #! record on|off   per-sweep records (shim build only)
      #! snap TAG        print the hash and all site values
      #! energy          print spparks_energy (only after a run)
+     #! timed TAG CMD   run the input command CMD and print its wall time
    Output lines:
      sweep N NACCEPT NATTEMPT HASH TIME
      snap TAG HASH NLOCAL v1 v2 ...
      energy E
+     timed TAG SECONDS
 */
 
 #include <cstdio>
@@ -22,6 +24,7 @@
 #include <string>
 #include <vector>
 #include <stdint.h>
+#include <time.h>
 
 #include "library.h"
 #include "../philox_oracle.h"
@@ -95,6 +98,19 @@ int main(int argc, char **argv) {
       } else if (!strcmp(cmd, "energy")) {
         // valid only after a run: spparks_energy needs the app's comm set up
         printf("energy %.17g\n", spparks_energy(spk));
+      } else if (!strcmp(cmd, "timed")) {
+        // the command is the rest of the line after the tag
+        const char *rest = strstr(line + 2, a1) + strlen(a1);
+        while (*rest == ' ') rest++;
+        char buf[4096];
+        snprintf(buf, sizeof(buf), "%s", rest);
+        timespec t0, t1;
+        clock_gettime(CLOCK_MONOTONIC, &t0);
+        spparks_command(spk, buf);
+        clock_gettime(CLOCK_MONOTONIC, &t1);
+        flush_records();
+        printf("timed %s %.9f\n", a1, (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec));
+        fflush(stdout);
       } else if (!strcmp(cmd, "record")) {
 #ifdef SPK_SHIM
         spk_oracle::record_on = !strcmp(a1, "on");

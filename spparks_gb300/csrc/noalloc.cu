@@ -22,10 +22,18 @@
 //
 // Host code cannot use the array's name as a device address (it names a host
 // shadow), so the first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current and caches it.  That
-// first call therefore does set-up work and should be made before any
-// stream capture.
+// cudaGetSymbolAddress while that device is current and caches it together
+// with the device's current context.  That first call therefore does set-up
+// work and should be made before any stream capture.  When the context
+// changes (after cudaDeviceReset the runtime makes a new primary context and
+// reloads the module), the next call looks the address up again, so a reset
+// never leaves a stale address behind.
+//
+// With naccept set, the call reads the counter back and waits for the
+// stream; that cannot be part of a stream capture, so such a call on a
+// capturing stream is refused (SPKGPU_ERR_ARG) before anything is enqueued.
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -42,18 +50,45 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kCounterBytes + SPKGPU
 
 constexpr int kMaxDevices = 64;
 void *g_scratch_ptr[kMaxDevices] = {nullptr};
+CUcontext g_scratch_ctx[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mutex;
 
-// address of the scratch array on the current device (looked up once)
+// the calling thread's current context (driver entry point reached through
+// the runtime, so the library does not link the driver library itself)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+int current_context(CUcontext *ctx) {
+  // looked up once (thread-safe static initialisation)
+  static const CtxGetCurrentFn fn = []() -> CtxGetCurrentFn {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return (CtxGetCurrentFn)p;
+  }();
+  if (!fn) return SPKGPU_ERR_CUDA;
+  return fn(ctx) == CUDA_SUCCESS && *ctx ? SPKGPU_OK : SPKGPU_ERR_CUDA;
+}
+
+// address of the scratch array on the current device, looked up once per
+// device and context
 int scratch_on_current_device(unsigned char **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return SPKGPU_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return SPKGPU_ERR_UNSUPPORTED;
+  CUcontext ctx = nullptr;
+  if (current_context(&ctx) != SPKGPU_OK) {
+    // no context bound to this thread yet: bind the device's primary context
+    if (cudaSetDevice(dev) != cudaSuccess) return SPKGPU_ERR_CUDA;
+    int rc = current_context(&ctx);
+    if (rc) return rc;
+  }
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SPKGPU_ERR_CUDA;
     g_scratch_ptr[dev] = p;
+    g_scratch_ctx[dev] = ctx;
   }
   *out = (unsigned char *)g_scratch_ptr[dev];
   return SPKGPU_OK;
@@ -76,12 +111,18 @@ extern "C" int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int3
   size_t bytes = (size_t)nx * (size_t)ny * (size_t)spin_bytes;
   if (bytes > (size_t)SPKGPU_NOALLOC_MAX_BYTES) return SPKGPU_ERR_TOO_LARGE;
 
+  cudaStream_t s = (cudaStream_t)stream;
+  if (naccept) {
+    // reading the counter back waits for the stream: not possible in a capture
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return SPKGPU_ERR_CUDA;
+    if (cap != cudaStreamCaptureStatusNone) return SPKGPU_ERR_ARG;
+  }
   unsigned char *scratch = nullptr;
   int rc = scratch_on_current_device(&scratch);
   if (rc) return rc;
   unsigned long long *counter = (unsigned long long *)scratch;
   void *other = scratch + kCounterBytes;
-  cudaStream_t s = (cudaStream_t)stream;
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

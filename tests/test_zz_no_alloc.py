@@ -18,7 +18,8 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 
-TOO_LARGE = -8
+ERR_ARG, TOO_LARGE = -1, -8
+NOALLOC_MAX_BYTES = 4 << 20  # SPKGPU_NOALLOC_MAX_BYTES
 
 
 @pytest.fixture(scope="module")
@@ -76,3 +77,77 @@ def test_noalloc_rejects_lattices_beyond_the_static_array(lib):
     rc = lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(16), 4096, 2048, 1, sg.ISING, 2, 2.0, 1, 0, 1, None,
                                       ctypes.byref(na))
     assert rc == TOO_LARGE
+
+
+def _regular(app, q, T, nx, ny, sb, seed, spin, nsweeps):
+    import spparks_gb300 as sg
+
+    ref = sg.Lattice("sq/4n", nx, ny, 1, app, q, spin_bytes=sb, seed=seed)
+    ref.set_temperature(T)
+    ref.upload(spin)
+    ref.sweep(nsweeps)
+    out, na = ref.download(), ref.stats()["naccept"]
+    ref.close()
+    return out, na
+
+
+def test_noalloc_at_the_size_limit_and_without_waiting(lib):
+    """A 2048 x 2048 int8 lattice fills the static array exactly and is
+    accepted.  Three sweeps run on a side stream with naccept = NULL (the call
+    returns without waiting); a zero-sweep call then changes nothing and
+    reports zero."""
+    import torch
+
+    import spparks_gb300 as sg
+
+    nx = ny = 2048
+    assert nx * ny == NOALLOC_MAX_BYTES
+    seed, T = 1357, 2.269
+    spin = oracle.init_spins(seed, nx * ny, 1, 2)
+    dev = torch.from_numpy(spin).to(torch.int8).cuda()
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    rc = lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(dev.data_ptr()), nx, ny, 1, sg.ISING, 2, T, seed, 0, 3,
+                                      ctypes.c_void_p(side.cuda_stream), None)
+    assert rc == 0
+    side.synchronize()
+    want, _ = _regular("ising", 2, T, nx, ny, 1, seed, spin, 3)
+    got = dev.to(torch.int32).cpu().numpy()
+    assert np.array_equal(got, want)
+    na = ctypes.c_int64(-1)
+    rc = lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(dev.data_ptr()), nx, ny, 1, sg.ISING, 2, T, seed, 3, 0,
+                                      ctypes.c_void_p(side.cuda_stream), ctypes.byref(na))
+    assert rc == 0 and na.value == 0
+    assert np.array_equal(dev.to(torch.int32).cpu().numpy(), want)
+
+
+def test_noalloc_refuses_a_counter_read_inside_a_capture(lib):
+    """Reading the change count back waits for the stream, which a stream
+    capture cannot hold: the call is refused before it enqueues anything,
+    and the same call without the counter is then captured and replayed."""
+    import torch
+
+    import spparks_gb300 as sg
+
+    nx, ny, seed, T = 64, 64, 97, 2.0
+    spin = oracle.init_spins(seed, nx * ny, 1, 2)
+    dev = torch.from_numpy(spin).to(torch.int8).cuda()
+    na = ctypes.c_int64(-1)
+    # the set-up call (address lookup) before any capture
+    assert lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(dev.data_ptr()), nx, ny, 1, sg.ISING, 2, T, seed, 0, 0,
+                                        None, ctypes.byref(na)) == 0
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        refused = lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(dev.data_ptr()), nx, ny, 1, sg.ISING, 2, T, seed,
+                                               0, 2, ctypes.c_void_p(side.cuda_stream), ctypes.byref(na))
+        captured = lib.spkgpu_sweep_sq4_noalloc(ctypes.c_void_p(dev.data_ptr()), nx, ny, 1, sg.ISING, 2, T, seed,
+                                                0, 2, ctypes.c_void_p(side.cuda_stream), None)
+    assert refused == ERR_ARG and captured == 0
+    # the capture recorded the work without running it
+    assert np.array_equal(dev.to(torch.int32).cpu().numpy(), spin)
+    g.replay()
+    torch.cuda.synchronize()
+    want, _ = _regular("ising", 2, T, nx, ny, 1, seed, spin, 2)
+    assert np.array_equal(dev.to(torch.int32).cpu().numpy(), want)
