@@ -113,6 +113,8 @@ def lib():
         L.spko_philox.argtypes = [P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_uint32)]
         L.spko_neighbors.argtypes = [P(Cfg), ctypes.c_int64, i64p]
         L.spko_neighbors.restype = ctypes.c_int
+        L.spko_maxneigh.argtypes = [ctypes.c_int]
+        L.spko_maxneigh.restype = ctypes.c_int
         L.spko_color.argtypes = [P(Cfg), ctypes.c_int64]
         L.spko_sector.argtypes = [P(Cfg), ctypes.c_int64]
         L.spko_energy.argtypes = [P(Cfg), i32p]
@@ -125,6 +127,11 @@ def lib():
         L.spko_color_sweeps.argtypes = [P(Cfg), i32p, ctypes.c_int64, ctypes.c_int, i64p, i64p, u64p,
                                         i32p, u8p]
         L.spko_color_sweeps.restype = ctypes.c_int
+        L.spko_init_values.argtypes = [ctypes.c_uint32, ctypes.c_int64, i64p, ctypes.c_int, ctypes.c_int, i32p]
+        L.spko_site_updates.argtypes = [P(Cfg), ctypes.c_int64, i64p, i32p, i32p, ctypes.c_uint32,
+                                        ctypes.c_uint32, i32p]
+        L.spko_site_updates.restype = ctypes.c_int64
+        L.spko_neighbors_many.argtypes = [P(Cfg), ctypes.c_int64, i64p, i64p]
         L.spko_ranmars_init.argtypes = [P(RanMars), ctypes.c_int]
         L.spko_ranmars_uniform.argtypes = [P(RanMars)]
         L.spko_ranmars_uniform.restype = ctypes.c_double
@@ -179,6 +186,14 @@ def init_spins(seed: int, n: int, lo: int, hi: int) -> np.ndarray:
     return s
 
 
+def init_values(seed: int, ids: np.ndarray, lo: int, hi: int) -> np.ndarray:
+    """The initial values init_spins gives the sites `ids` alone."""
+    ids = np.ascontiguousarray(ids, dtype=np.int64)
+    out = np.empty(ids.size, dtype=np.int32)
+    lib().spko_init_values(seed & 0xFFFFFFFF, ids.size, _ptr(ids, ctypes.c_int64), lo, hi, _ptr(out, ctypes.c_int32))
+    return out
+
+
 def neighbors(cfg: Cfg, i: int) -> list[int]:
     out = (ctypes.c_int64 * 26)()
     n = lib().spko_neighbors(ctypes.byref(cfg), i, out)
@@ -198,6 +213,29 @@ def color_sweeps(cfg: Cfg, spin: np.ndarray, sweep0: int, nsweeps: int, siteseed
     if rc != 0:
         raise RuntimeError(f"oracle colour sweep failed: {rc}")
     return na.value, nt.value, hashes[:nsweeps]
+
+
+def neighbors_many(cfg: Cfg, ids: np.ndarray) -> np.ndarray:
+    """Neighbour ids of many sites, shape (n, maxneigh), reference order."""
+    ids = np.ascontiguousarray(ids, dtype=np.int64)
+    nn = lib().spko_maxneigh(cfg.lattice)
+    out = np.empty((ids.size, nn), dtype=np.int64)
+    lib().spko_neighbors_many(ctypes.byref(cfg), ids.size, _ptr(ids, ctypes.c_int64), _ptr(out, ctypes.c_int64))
+    return out
+
+
+def site_updates(cfg: Cfg, ids: np.ndarray, self_vals: np.ndarray, nbr_vals: np.ndarray, sweep: int,
+                 npass: int = 0) -> np.ndarray:
+    """New values of sites `ids` after their visit in colour sweep `sweep`,
+    given their own values and their neighbours' values (n, maxneigh) as
+    they see them at their turn."""
+    ids = np.ascontiguousarray(ids, dtype=np.int64)
+    sv = np.ascontiguousarray(self_vals, dtype=np.int32)
+    nv = np.ascontiguousarray(nbr_vals, dtype=np.int32)
+    out = np.empty(ids.size, dtype=np.int32)
+    lib().spko_site_updates(ctypes.byref(cfg), ids.size, _ptr(ids, ctypes.c_int64), _ptr(sv, ctypes.c_int32),
+                            _ptr(nv, ctypes.c_int32), sweep, npass, _ptr(out, ctypes.c_int32))
+    return out
 
 
 def energy(cfg: Cfg, spin: np.ndarray) -> float:
@@ -285,6 +323,15 @@ def bonds_sq4(spin2d: np.ndarray) -> int:
     return int(np.sum(s != np.roll(s, -1, axis=1)) + np.sum(s != np.roll(s, -1, axis=0)))
 
 
+def _ensemble_block(job):
+    """n colour sweeps of one ensemble replica from sweep index sweep0 (one
+    process-pool task of EnsembleOracle.run); returns (sites, naccept)."""
+    L, app, nspins, T, seed, stream_base, sp, sweep0, n = job
+    cfg = make_cfg("sq/4n", L, L, 1, app, nspins, T, seed=seed, stream_base=stream_base)
+    na, _, _ = color_sweeps(cfg, sp, sweep0, n)
+    return sp, na
+
+
 class EnsembleOracle:
     """Restatement of the batched ensemble: every replica follows the oracle's
     sq/4n colour sweep with Philox stream (r+1) << 8; every `every` sweeps the
@@ -318,30 +365,48 @@ class EnsembleOracle:
         self.accepts = 0
         self.last_bonds = [0] * n
 
-    def run(self, spins: list, nsweeps: int):
-        for _ in range(nsweeps):
-            for r, sp in enumerate(spins):
-                cfg = make_cfg("sq/4n", self.L[r], self.L[r], 1, self.app, self.nspins, self.T0[self.tidx[r]],
-                               seed=self.seed, stream_base=(r + 1) << 8)
-                na, _, _ = color_sweeps(cfg, sp, self.sweep, 1)
+    def run(self, spins: list, nsweeps: int, pool=None):
+        """Runs nsweeps sweeps of every replica in place, with the exchange
+        rounds that fall inside them.  Between two rounds the replicas are
+        independent and keep their temperatures, so each replica's sweeps up
+        to the next round are one oracle call; `pool` (a multiprocessing pool
+        started with spawn) spreads those calls over processes."""
+        done = 0
+        while done < nsweeps:
+            n = nsweeps - done
+            if self.every:
+                n = min(n, self.every - self.sweep % self.every)
+            jobs = [(self.L[r], self.app, self.nspins, self.T0[self.tidx[r]], self.seed, (r + 1) << 8, sp,
+                     self.sweep, n) for r, sp in enumerate(spins)]
+            if pool is None:
+                res = [_ensemble_block(j) for j in jobs]
+            else:
+                res = pool.map(_ensemble_block, jobs, chunksize=1)
+            for r, (sp, na) in enumerate(res):
+                if pool is not None:
+                    spins[r][...] = sp
                 self.naccept += na
-            self.sweep += 1
+            self.sweep += n
+            done += n
             if self.every and self.sweep % self.every == 0:
-                bonds = [bonds_sq4(sp.reshape(self.L[r], self.L[r])) for r, sp in enumerate(spins)]
-                for g, (slots_t, who) in enumerate(zip(self.slot_t, self.who)):
-                    for j in range(self.xround & 1, len(who) - 1, 2):
-                        ra, rb = who[j], who[j + 1]
-                        ta, tb = slots_t[j], slots_t[j + 1]
-                        delta = (1.0 / self.T0[ta] - 1.0 / self.T0[tb]) * (float(bonds[ra]) - float(bonds[rb]))
-                        x = philox([self.xround, g, j, 0], [self.seed & 0xFFFFFFFF, 2])[0]
-                        ok = delta >= 0.0 or float(x) < self.math.floor(self.math.exp(delta) * 4294967296.0)
-                        self.tries += 1
-                        if ok:
-                            who[j], who[j + 1] = rb, ra
-                            self.tidx[ra], self.tidx[rb] = tb, ta
-                            self.accepts += 1
-                self.last_bonds = bonds
-                self.xround += 1
+                self._exchange(spins)
+
+    def _exchange(self, spins):
+        bonds = [bonds_sq4(sp.reshape(self.L[r], self.L[r])) for r, sp in enumerate(spins)]
+        for g, (slots_t, who) in enumerate(zip(self.slot_t, self.who)):
+            for j in range(self.xround & 1, len(who) - 1, 2):
+                ra, rb = who[j], who[j + 1]
+                ta, tb = slots_t[j], slots_t[j + 1]
+                delta = (1.0 / self.T0[ta] - 1.0 / self.T0[tb]) * (float(bonds[ra]) - float(bonds[rb]))
+                x = philox([self.xround, g, j, 0], [self.seed & 0xFFFFFFFF, 2])[0]
+                ok = delta >= 0.0 or float(x) < self.math.floor(self.math.exp(delta) * 4294967296.0)
+                self.tries += 1
+                if ok:
+                    who[j], who[j + 1] = rb, ra
+                    self.tidx[ra], self.tidx[rb] = tb, ta
+                    self.accepts += 1
+        self.last_bonds = bonds
+        self.xround += 1
 
     def temperatures(self):
         return [self.T0[t] for t in self.tidx]

@@ -54,7 +54,7 @@ void PhiloxApp<Base>::site_event_rejection(int i, RandomPark *random) {
   const int sh = ising ? 2 : 1;
   uint32_t ctr[4] = {(uint32_t)(s >> sh), (uint32_t)(s >> (32 + sh)), (uint32_t)this->nsweeps,
                      (uint32_t)visits[i]};
-  uint32_t key[2] = {spk_shim::philox_seed, SPKO_STREAM_SWEEP};
+  uint32_t key[2] = {spk_shim::philox_seed, spk_shim::stream_base | SPKO_STREAM_SWEEP};
   spk_shim::DrawCtx &c = spk_shim::ctx;
   spko_philox4x32_10(ctr, key, c.w);
   c.base = ising ? (int)(s & 3) : (int)(s & 1) * 2;

@@ -6,6 +6,8 @@
    usage: ref_runner SCRIPT
    SCRIPT holds reference input commands, one per line, plus directives:
      #! seed S          Philox key for the shim build and for init_spins
+     #! stream B        stream word base of the sweep draws (shim build;
+                        replica r of an ensemble uses (r+1) << 8)
      #! init_spins LO HI  overwrite site values with Philox initial spins
      #! record on|off   per-sweep records (shim build only)
      #! snap TAG        print the hash and all site values
@@ -87,6 +89,10 @@ int main(int argc, char **argv) {
         seed = (uint32_t)strtoul(a1, NULL, 10);
 #ifdef SPK_SHIM
         spk_shim::philox_seed = seed;
+#endif
+      } else if (!strcmp(cmd, "stream")) {
+#ifdef SPK_SHIM
+        spk_shim::stream_base = (uint32_t)strtoul(a1, NULL, 10);
 #endif
       } else if (!strcmp(cmd, "init_spins")) {
         int lo = atoi(a1), hi = atoi(a2);

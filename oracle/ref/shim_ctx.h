@@ -18,6 +18,8 @@ struct DrawCtx {
 
 extern DrawCtx ctx;
 extern uint32_t philox_seed;
+// high bits of the Philox key's stream word (replica r of an ensemble: (r+1) << 8)
+extern uint32_t stream_base;
 
 }  // namespace spk_shim
 

@@ -24,6 +24,7 @@ using namespace SPPARKS_NS;
 namespace spk_shim {
 DrawCtx ctx = {0, {0, 0, 0, 0}, 0, 0, 0, 0};
 uint32_t philox_seed = 12345;
+uint32_t stream_base = 0;
 }  // namespace spk_shim
 
 static const int kIA = 16807;

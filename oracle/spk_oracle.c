@@ -177,6 +177,10 @@ void spko_init_spins(uint32_t seed, int64_t n, int lo, int hi, int32_t *spin) {
   for (int64_t i = 0; i < n; i++) spin[i] = spko_init_spin(seed, (uint64_t)i, lo, hi);
 }
 
+void spko_init_values(uint32_t seed, int64_t n, const int64_t *ids, int lo, int hi, int32_t *out) {
+  for (int64_t k = 0; k < n; k++) out[k] = spko_init_spin(seed, (uint64_t)ids[k], lo, hi);
+}
+
 static int64_t nsites(const spko_cfg *c) { return (int64_t)c->nx * c->ny * c->nz; }
 
 /* site_energy: count of unlike neighbours
@@ -372,6 +376,40 @@ static int site_event_rejection(const spko_cfg *c, int32_t *spin, int64_t i, dra
   int64_t nb[26];
   int nn = spko_neighbors(c, i, nb);
   return site_event_rejection_nb(c, spin, i, nb, nn, d, mask);
+}
+
+/* the per-site rule of one colour-sweep visit, applied to sites given with
+   the values they see (site_event_rejection_nb on a local copy) */
+int64_t spko_site_updates(const spko_cfg *c, int64_t n, const int64_t *ids, const int32_t *self,
+                          const int32_t *nbv, uint32_t sweep, uint32_t pass, int32_t *out) {
+  int nn = spko_maxneigh(c->lattice);
+  int64_t nb[26];
+  int32_t local[27];
+  int64_t changed = 0;
+  for (int j = 0; j < nn; j++) nb[j] = j + 1;
+  for (int64_t k = 0; k < n; k++) {
+    local[0] = self[k];
+    for (int j = 0; j < nn; j++) local[j + 1] = nbv[k * nn + j];
+    draw_src d;
+    d.mode = SPKO_RNG_PHILOX;
+    d.used = 0;
+    d.ising = 0;
+    d.park = NULL;
+    if (c->app == SPKO_ISING) {
+      d.x[0] = d.x[1] = spko_ising_word(c->seed, c->stream_base, (uint64_t)ids[k], sweep, pass);
+      d.ising = 1;
+    } else {
+      spko_site_draws(c->seed, c->stream_base, (uint64_t)ids[k], sweep, pass, &d.x[0], &d.x[1]);
+    }
+    changed += site_event_rejection_nb(c, local, 0, nb, nn, &d, NULL);
+    out[k] = local[0];
+  }
+  return changed;
+}
+
+void spko_neighbors_many(const spko_cfg *c, int64_t n, const int64_t *ids, int64_t *out) {
+  int nn = spko_maxneigh(c->lattice);
+  for (int64_t k = 0; k < n; k++) spko_neighbors(c, ids[k], out + k * nn);
 }
 
 /* ---------------------------------------------------------------------- */

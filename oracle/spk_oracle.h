@@ -44,6 +44,8 @@ int spko_clusters(const spko_cfg *c, const int32_t *spin, int64_t *ncluster, dou
 uint64_t spko_hash(const int32_t *spin, int64_t n);
 void spko_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 void spko_init_spins(uint32_t seed, int64_t n, int lo, int hi, int32_t *spin);
+/* the initial values of the sites ids[0..n-1] alone (as spko_init_spins) */
+void spko_init_values(uint32_t seed, int64_t n, const int64_t *ids, int lo, int hi, int32_t *out);
 
 /* Rejection (rKMC) colour sweeps.  Runs nsweeps sweeps starting at sweep
    index sweep0.  naccept/nattempt accumulate; hashes (optional) receive the
@@ -52,6 +54,16 @@ void spko_init_spins(uint32_t seed, int64_t n, int lo, int hi, int32_t *spin);
 int spko_color_sweeps(const spko_cfg *c, int32_t *spin, int64_t sweep0, int nsweeps,
                       int64_t *naccept, int64_t *nattempt, uint64_t *hashes,
                       int32_t *siteseeds, uint8_t *mask);
+
+/* Single site updates for lattices too large for a full oracle run: site
+   ids[k] with value self[k] and its neighbours' values nbv[k*nn .. k*nn+nn-1]
+   (nn = maxneigh, in spko_neighbors order) as the site sees them at its turn
+   in colour sweep `sweep`, pass `pass` (Philox draws); out[k] = its value
+   after its site_event_rejection.  Returns the number of changed sites. */
+int64_t spko_site_updates(const spko_cfg *c, int64_t n, const int64_t *ids, const int32_t *self,
+                          const int32_t *nbv, uint32_t sweep, uint32_t pass, int32_t *out);
+/* neighbour ids of n sites, nn = maxneigh per site (spko_neighbors order) */
+void spko_neighbors_many(const spko_cfg *c, int64_t n, const int64_t *ids, int64_t *out);
 
 /* Park-Miller / Marsaglia restatements for the reference's own seeding */
 typedef struct {

@@ -11,6 +11,12 @@ if str(ROOT) not in sys.path:
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
+def fixture_count(group: str) -> int:
+    """Number of reference fixtures in a group of reference_philox.json (for
+    parametrising tests at collection time)."""
+    return len(json.loads((GOLDEN / "reference_philox.json").read_text())[group])
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
 

@@ -55,7 +55,13 @@ def sweep_script(case):
     c = case
     lines = ["seed 56789", app_line(c["app"], c["nspins"])]
     lines += geometry_lines(c["lattice"], c["nx"], c["ny"], c["nz"])
-    lines += [f"#! seed {c['seed']}", f"#! init_spins 1 {c['nspins']}", "#! snap init"]
+    if "init_seed" in c:
+        lines += [f"#! seed {c['init_seed']}", f"#! init_spins 1 {c['nspins']}", "#! snap init",
+                  f"#! seed {c['seed']}"]
+    else:
+        lines += [f"#! seed {c['seed']}", f"#! init_spins 1 {c['nspins']}", "#! snap init"]
+    if "stream_base" in c:
+        lines.append(f"#! stream {c['stream_base']}")
     lines.append("sweep color" + (" mask yes" if c.get("mask") else ""))
     if c.get("nsector", 1) > 1:
         s = "sector yes" if c["nsector"] in (4, 8) and not c.get("nsector_explicit") else f"sector {c['nsector']}"
@@ -157,6 +163,24 @@ SWEEP_CASES = [
          temperature=1.0, seed=34, nsweeps=3),
     dict(name="neighonly_sq8n_Q1", app="potts/neighonly", nspins=1, lattice="sq/8n", nx=8, ny=8, nz=1,
          temperature=0.5, seed=35, nsweeps=3),
+    # lattices the int8 warp tile takes (sides multiples of 32): the single-lattice warp sweep is pinned to
+    # the reference directly
+    dict(name="ising_sq4n_64_T2269", app="ising", nspins=2, lattice="sq/4n", nx=64, ny=64, nz=1,
+         temperature=2.269, seed=56789, nsweeps=8),
+    dict(name="ising_sq4n_96x64_T19", app="ising", nspins=2, lattice="sq/4n", nx=96, ny=64, nz=1,
+         temperature=1.9, seed=4242, nsweeps=6),
+]
+
+# replicas of a batched ensemble (no exchange): replica r draws from Philox stream word (r+1) << 8, so the
+# ensemble's warp-tile sweep is pinned to the reference directly
+ENSEMBLE_SEED = 31
+ENSEMBLE_CASES = [
+    dict(name="ensemble_r0_ising_64_T20", app="ising", nspins=2, lattice="sq/4n", nx=64, ny=64, nz=1,
+         temperature=2.0, seed=ENSEMBLE_SEED, init_seed=701, stream_base=1 << 8, nsweeps=6),
+    dict(name="ensemble_r1_ising_96_T26", app="ising", nspins=2, lattice="sq/4n", nx=96, ny=96, nz=1,
+         temperature=2.6, seed=ENSEMBLE_SEED, init_seed=702, stream_base=2 << 8, nsweeps=6),
+    dict(name="ensemble_r2_ising_32_T15", app="ising", nspins=2, lattice="sq/4n", nx=32, ny=32, nz=1,
+         temperature=1.5, seed=ENSEMBLE_SEED, init_seed=703, stream_base=3 << 8, nsweeps=6),
 ]
 
 KMC_CASES = [
@@ -356,13 +380,14 @@ def main():
     philox = ROOT / "oracle" / "_ref" / "runner_philox"
     plain = ROOT / "oracle" / "_ref" / "runner_plain"
 
-    fixtures = {"sweeps": [], "kmc": [], "strict": []}
-    for case in SWEEP_CASES:
-        lines = sweep_script(case)
-        res = run_runner(philox, lines)
-        assert len(res["sweeps"]) == case["nsweeps"], (case["name"], len(res["sweeps"]))
-        fixtures["sweeps"].append({"case": case, "script": lines, **res})
-        print("sweep case", case["name"], "final", res["snaps"]["final"]["hash"])
+    fixtures = {"sweeps": [], "kmc": [], "strict": [], "ensemble": []}
+    for group, cases in (("sweeps", SWEEP_CASES), ("ensemble", ENSEMBLE_CASES)):
+        for case in cases:
+            lines = sweep_script(case)
+            res = run_runner(philox, lines)
+            assert len(res["sweeps"]) == case["nsweeps"], (case["name"], len(res["sweeps"]))
+            fixtures[group].append({"case": case, "script": lines, **res})
+            print(group, "case", case["name"], "final", res["snaps"]["final"]["hash"])
     for case in KMC_CASES:
         lines = kmc_script(case)
         res = run_runner(philox, lines)

@@ -187,3 +187,29 @@ def test_run_io_reports_invalid_input_at_synchronize(sg):
     assert ei.value.code == -6  # SPKGPU_ERR_INVALID_SPIN
     ens.synchronize()  # the flag is cleared once reported
     ens.close()
+
+
+def test_ensemble_replicas_match_reference_fixtures(sg, ref_fixtures, monkeypatch):
+    """replicas of one ensemble (no exchange) against the reference built
+    with the Philox shim and driven by each replica's stream word: every
+    execution form, the headline warp tile included, bit-identical after
+    every sweep"""
+    fxs = ref_fixtures["ensemble"]
+    cases = [fx["case"] for fx in fxs]
+    L = [c["nx"] for c in cases]
+    T = [c["temperature"] for c in cases]
+    assert all(c["stream_base"] == (r + 1) << 8 and c["seed"] == cases[0]["seed"] for r, c in enumerate(cases))
+    init = np.concatenate([np.array(fx["snaps"]["init"]["spins"], dtype=np.int32) for fx in fxs])
+    nsweeps = cases[0]["nsweeps"]
+    for mode in sg.ENSEMBLE_MODES:
+        monkeypatch.setenv("SPKGPU_ENSEMBLE_MODE", mode)
+        ens = sg.Ensemble(L, T, "ising", 2, seed=cases[0]["seed"], exchange_every=0)
+        assert ens.mode()["mode"] == mode
+        ens.upload(init)
+        for s in range(nsweeps):
+            ens.run(1)
+            out = ens.download()
+            for r, fx in enumerate(fxs):
+                assert format(oracle.spin_hash(ens.replica(out, r)), "016x") == fx["sweeps"][s][3], (mode, r, s)
+        assert ens.stats()["naccept"] == sum(fx["sweeps"][-1][1] for fx in fxs)
+        ens.close()

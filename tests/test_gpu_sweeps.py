@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import fixture_count
 
 pytestmark = pytest.mark.gpu
 
@@ -28,7 +29,7 @@ def make_lattice(sg, case, spin_bytes=0, rng=0, seed=None, procs=(1, 1, 1)):
                       seed=case.get("seed", 0) if seed is None else seed)
 
 
-@pytest.mark.parametrize("k", range(18))
+@pytest.mark.parametrize("k", range(fixture_count("sweeps")))
 def test_sweeps_match_reference_fixtures(sg, ref_fixtures, k):
     fx = ref_fixtures["sweeps"][k]
     case = fx["case"]

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import fixture_count
 
 # Philox4x32-10 known-answer vectors published with the Random123 library
 PHILOX_KAT = [
@@ -44,7 +45,7 @@ def test_neighbor_order_matches_reference_offsets():
     assert len(nb) == 26 and nb[0] == idx(3, 3, 3) and nb[-1] == idx(1, 1, 1)
 
 
-@pytest.mark.parametrize("k", range(18))
+@pytest.mark.parametrize("k", range(fixture_count("sweeps")))
 def test_sweeps_match_reference(ref_fixtures, k):
     fx = ref_fixtures["sweeps"][k]
     case = fx["case"]
@@ -57,6 +58,42 @@ def test_sweeps_match_reference(ref_fixtures, k):
     assert [format(int(h), "016x") for h in hashes] == [r[3] for r in ref]
     assert na == ref[-1][1] and nt == ref[-1][2]
     assert spin.tolist() == fx["snaps"]["final"]["spins"]
+
+
+@pytest.mark.parametrize("k", range(fixture_count("ensemble")))
+def test_ensemble_replicas_match_reference(ref_fixtures, k):
+    """a replica of a batched ensemble (its own Philox stream word) against
+    the reference driven by that stream"""
+    fx = ref_fixtures["ensemble"][k]
+    case = fx["case"]
+    cfg = oracle.make_cfg(case["lattice"], case["nx"], case["ny"], case["nz"], case["app"], case["nspins"],
+                          case["temperature"], seed=case["seed"], stream_base=case["stream_base"])
+    spin = np.array(fx["snaps"]["init"]["spins"], dtype=np.int32)
+    assert spin.tolist() == oracle.init_spins(case["init_seed"], spin.size, 1, case["nspins"]).tolist()
+    na, nt, hashes = oracle.color_sweeps(cfg, spin, 0, case["nsweeps"])
+    assert [format(int(h), "016x") for h in hashes] == [r[3] for r in fx["sweeps"]]
+    assert na == fx["sweeps"][-1][1] and nt == fx["sweeps"][-1][2]
+    assert spin.tolist() == fx["snaps"]["final"]["spins"]
+
+
+@pytest.mark.parametrize("lattice,nx,ny,nz,app,q,T", [
+    ("sc/6n", 8, 8, 8, "ising", 2, 4.5), ("sq/4n", 16, 8, 1, "ising", 2, 2.0), ("sq/8n", 16, 16, 1, "potts", 5, 1.0),
+    ("sc/26n", 6, 6, 6, "potts/neighonly", 9, 0.5), ("sq/4n", 8, 8, 1, "potts/neigh", 6, 0.7)])
+def test_single_site_updates_reproduce_a_colour_sweep(lattice, nx, ny, nz, app, q, T):
+    """the oracle's single-site rule, given each site's value and the values
+    its neighbours hold at its turn (lower colours already swept), gives the
+    same lattice as the oracle's whole colour sweep: the basis of the sampled
+    checks of lattices too large for a full oracle run"""
+    cfg = oracle.make_cfg(lattice, nx, ny, nz, app, q, T, seed=11)
+    n = nx * ny * nz
+    s0 = oracle.init_spins(11, n, 1, q)
+    s1 = s0.copy()
+    oracle.color_sweeps(cfg, s1, 3, 1)
+    ids = np.arange(n)
+    nb = oracle.neighbors_many(cfg, ids)
+    col = np.array([oracle.lib().spko_color(cfg, int(i)) for i in ids])
+    seen = np.where(col[nb] < col[:, None], s1[nb], s0[nb])
+    assert np.array_equal(oracle.site_updates(cfg, ids, s0, seen, 3), s1)
 
 
 @pytest.mark.parametrize("k", range(5))
