@@ -466,20 +466,26 @@ def run_ours(args):
     seq_ms = max_over_ranks((time.perf_counter() - t0) * 1e3, dist, f"cuda:{device}")
     e2e_seq_value = whole_job_rate(nsites * SWEEPS_PER_STEP * seq_steps, world, seq_ms)
 
-    # plain GPU sweep: the same replicas one by one with the per-colour phase
-    # kernel (a sample of replicas, 10 sweeps each, extrapolated by sites)
+    # plain GPU sweeps: the same replicas one lattice at a time (a sample of
+    # replicas, 10 sweeps each, extrapolated by sites), once with the generic
+    # per-colour phase kernel and once with the repo's fastest single-lattice
+    # sweep (the fused warp-tile kernel of spkgpu_sweep): batched over the
+    # latter measures what batching gains, over the former the kernel too
     rng = np.random.default_rng(11)
     pick = rng.choice(len(L), size=48, replace=False)
-    plain_ms, plain_sites = 0.0, 0
-    for r in pick:
-        lat = sg.Lattice("sq/4n", int(L[r]), int(L[r]), 1, "ising", 2, spin_bytes=1, seed=SEED, variant=1)
-        lat.set_temperature(float(T[r]))
-        lat.upload(ens.replica(spins, r))
-        lat.timed_sweeps(2)
-        plain_ms += lat.timed_sweeps(SWEEPS_PER_STEP)
-        plain_sites += int(L[r]) ** 2 * SWEEPS_PER_STEP
-        lat.close()
-    plain_rate = plain_sites / (plain_ms * 1e-3)
+    plain = {}
+    for variant in (1, 0):
+        plain_ms, plain_sites = 0.0, 0
+        for r in pick:
+            lat = sg.Lattice("sq/4n", int(L[r]), int(L[r]), 1, "ising", 2, spin_bytes=1, seed=SEED, variant=variant)
+            lat.set_temperature(float(T[r]))
+            lat.upload(ens.replica(spins, r))
+            lat.timed_sweeps(2)
+            plain_ms += lat.timed_sweeps(SWEEPS_PER_STEP)
+            plain_sites += int(L[r]) ** 2 * SWEEPS_PER_STEP
+            lat.close()
+        plain[variant] = plain_sites / (plain_ms * 1e-3)
+    plain_rate, plain_fused = plain[1], plain[0]
 
     peak, peak_kind = measured_peaks()
     # dominant kernel: the persistent kernel (all sweeps of a step) or the
@@ -496,7 +502,13 @@ def run_ours(args):
 
     if rank != 0:
         return
+    configs = measure_configs(sg, peak, peak_kind)
     cpu = None if args.no_cpu else cpu_baseline_leg()
+    if not args.no_cpu:
+        ref_cfg = reference_cpu_configs()
+        for name in ("C0", "C1", "C4"):
+            configs[name]["cpu_baseline"] = ref_cfg[name]
+        configs["C3_serial"]["cpu_baseline"] = ref_cfg["C3"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -514,7 +526,10 @@ def run_ours(args):
                                "api": "spkgpu_ensemble_upload + run + download per step"}},
         "gpu_launches": int(launches),
         "plain_gpu": {"value": plain_rate, "unit": UNIT, "sample": "48 replicas x 10 sweeps, per-colour "
-                      "phase kernel, one lattice at a time", "batched_over_plain": value / world / plain_rate},
+                      "phase kernel, one lattice at a time", "batched_over_plain": value / world / plain_rate,
+                      "fused": {"value": plain_fused, "unit": UNIT,
+                                "sample": "the same 48 replicas x 10 sweeps, fused warp-tile sweep (spkgpu_sweep), "
+                                          "one lattice at a time", "batched_over_plain": value / world / plain_fused}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} copy bandwidth (burst)", "traffic": traffic,
                      "traffic_source": traffic_src,
@@ -525,10 +540,156 @@ def run_ours(args):
                         "frac": value / world / (4.0 * philox_bps),
                         "source": "spkgpu_philox_rate: the sweeps' Philox code alone, 4 Ising sites per block"},
         "cpu_baseline": cpu,
+        "configs": configs,
         "clocks": clk,
         "exchange": {"tries": st["exchange_tries"], "accepts": st["exchange_accepts"]},
     }
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# The other configurations: each timed on the GPU (CUDA events on the
+# lattice's stream, or the host clock around a synchronous KMC run) and, on
+# one host core each, the reference itself on a bounded sample (run side by
+# side, one process per configuration).
+
+# (label, lattice, n, app, nspins, spin bytes, kT): the single-lattice sweeps
+C0 = ("sq/4n", (128, 128, 1), "ising", 2, 4, 2.269)
+C1 = ("sc/26n", (256, 256, 256), "potts/neighonly", 100, 2, 0.5)
+C4 = ("sc/6n", (1536, 1536, 1536), "ising", 2, -1, 4.5115)
+BYTES_PER_UPDATE = {4: 8.0, 2: 4.0, 1: 2.0, -1: 0.25}  # 2 s per site-update, s = storage bytes
+
+
+def _reference_lines(lattice, n, app, q, T, tail):
+    nx, ny, nz = n
+    dim = 3 if lattice.startswith("sc") else 2
+    zr = f"0 {nz}" if dim == 3 else "-0.5 0.5"
+    app_line = "app_style ising" if app == "ising" else f"app_style {app} {q}"
+    return [f"seed {SEED}", app_line, f"dimension {dim}", f"lattice {lattice} 1.0",
+            f"region box block 0 {nx} 0 {ny} {zr}", "create_box box", "create_sites box",
+            f"set site range 1 {q}"] + tail
+
+
+REF_CPU_CASES = {
+    # 100 sweeps of 128^2, 40 times (dt_sweep = 1/2 for ising)
+    "C0": dict(lines=_reference_lines("sq/4n", (128, 128, 1), "ising", 2, 2.269,
+                                      ["sweep color", "temperature 2.269"] +
+                                      [f"#! timed {k} run 50" for k in range(40)]),
+               updates=128 * 128 * 100 * 40, sample="128^2 sq/4n ising kT 2.269, 40 x 100 sweeps"),
+    # 96^3 sc/26n potts/neighonly Q=100: 12 sweeps (dt_sweep = 1/26; the run stops half a sweep early)
+    "C1": dict(lines=_reference_lines("sc/26n", (96, 96, 96), "potts/neighonly", 100, 0.5,
+                                      ["sweep color", "temperature 0.5", f"#! timed 0 run {11.5 / 26!r}"]),
+               updates=96 ** 3 * 12, sample="96^3 sc/26n potts/neighonly Q=100 kT 0.5, 12 sweeps"),
+    # 2048^2 sq/8n potts Q=50, solve_style tree with sector yes, serial: events to t = 0.03
+    "C3": dict(lines=_reference_lines("sq/8n", (2048, 2048, 1), "potts", 50, 1.0,
+                                      ["solve_style tree", "sector yes", "temperature 1.0", "#! timed 0 run 0.03",
+                                       "#! appstats"]),
+               updates=None, sample="2048^2 sq/8n potts Q=50 kT 1, tree, 4 sectors, one processor, to t = 0.03"),
+    # 128^3 sc/6n ising (the full 1536^3 lattice does not fit a CPU run): 16 sweeps
+    "C4": dict(lines=_reference_lines("sc/6n", (128, 128, 128), "ising", 2, 4.5115,
+                                      ["sweep color", "temperature 4.5115", "#! timed 0 run 8"]),
+               updates=128 ** 3 * 16, sample="128^3 sc/6n ising kT 4.5115, 16 sweeps"),
+}
+
+
+def reference_cpu_configs():
+    """The reference on one host core per configuration, all at once."""
+    binary, why = reference_binary()
+    if not binary:
+        return {k: {"unavailable": why} for k in REF_CPU_CASES}
+    tmpdir = Path(tempfile.mkdtemp(prefix="spk_refcfg_"))
+    procs = {}
+    for name, case in REF_CPU_CASES.items():
+        f = tmpdir / f"in.{name}"
+        f.write_text("\n".join(case["lines"]) + "\n")
+        procs[name] = subprocess.Popen([str(binary), str(f)], stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                                       text=True, cwd=str(tmpdir))
+    out = {}
+    for name, pr in procs.items():
+        o, e = pr.communicate()
+        case = REF_CPU_CASES[name]
+        if pr.returncode != 0:
+            out[name] = {"unavailable": f"reference run failed: {e[-200:]}"}
+            continue
+        secs = sum(float(l.split()[2]) for l in o.splitlines() if l.startswith("timed "))
+        if case["updates"] is None:  # KMC: events from the app's own stats line
+            st = [l.split() for l in o.splitlines() if l.startswith("appstats ")][-1]
+            units, unit = int(st[2]), "events/s"
+        else:
+            units, unit = case["updates"], UNIT
+        out[name] = {"value": units / secs, "unit": unit, "cores": 1, "kind": "reference",
+                     "sample": f"{case['sample']} ({units:.3g} in {secs:.1f} s), SPPARKS built from its own sources "
+                               "on this host, stock RandomPark"}
+        (tmpdir / f"in.{name}").unlink()
+    tmpdir.rmdir()
+    return out
+
+
+def _sweep_rate(sg, cfg, nsweeps, warm=1, seed=SEED, variant=0):
+    lattice, n, app, q, sb, T = cfg
+    lat = sg.Lattice(lattice, *n, app, q, spin_bytes=sb, seed=seed, variant=variant)
+    lat.set_temperature(T)
+    lat.init_spins(1, q)
+    lat.timed_sweeps(warm)
+    ms = lat.timed_sweeps(nsweeps)
+    sites = lat.n
+    launches = lat.launch_count()
+    lat.close()
+    return sites * nsweeps / (ms * 1e-3), ms / nsweeps, launches
+
+
+def _roofline(rate, bytes_per_update, peak, peak_kind, bound="hbm"):
+    achieved = rate * bytes_per_update / 1e9
+    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": f"{peak_kind} copy bandwidth", "bytes_per_update": bytes_per_update}
+
+
+def measure_configs(sg, peak, peak_kind):
+    """GPU rates of C0, C1, C3 (serial and processor grid) and C4 (bit-packed
+    and int8 on the same lattice), each on its own stream."""
+    res = {}
+    r, ms, _ = _sweep_rate(sg, C0, 100, warm=5)
+    res["C0"] = {"workload": "128^2 sq/4n ising int32 kT 2.269, 100 sweeps (the whole job)", "value": r,
+                 "unit": UNIT, "ms_per_sweep": ms,
+                 "roofline": {**_roofline(r, 8.0, peak, peak_kind, "latency"),
+                              "note": "64 KB lattice, L2-resident: the launch sequence bounds it, not HBM"}}
+    r, ms, _ = _sweep_rate(sg, C1, 20, warm=2)
+    res["C1"] = {"workload": "256^3 sc/26n potts/neighonly Q=100 int16 kT 0.5, 20 of the 1000 sweeps", "value": r,
+                 "unit": UNIT, "ms_per_sweep": ms, "roofline": _roofline(r, 4.0, peak, peak_kind, "alu")}
+    rp, msp, _ = _sweep_rate(sg, C4, 5)
+    r8, ms8, _ = _sweep_rate(sg, C4[:4] + (1,) + C4[5:], 2)
+    res["C4"] = {"workload": "1536^3 sc/6n ising kT 4.5115 (3.6e9 sites), 5 of the 500 sweeps", "value": rp,
+                 "unit": UNIT, "ms_per_sweep": msp, "roofline": _roofline(rp, 0.25, peak, peak_kind, "alu"),
+                 "int8_same_lattice": {"value": r8, "unit": UNIT, "ms_per_sweep": ms8,
+                                       "roofline": _roofline(r8, 2.0, peak, peak_kind),
+                                       "kernel": "per-colour phase kernel, int8"},
+                 "packed_over_int8": rp / r8}
+    for name, procs, tend in (("C3_serial", (1, 1, 1), 0.01), ("C3_grid", (32, 32, 1), 1.0)):
+        lat = sg.Lattice("sq/8n", 2048, 2048, 1, "potts", 50, spin_bytes=4, nsector=4, procs=procs, seed=SEED)
+        lat.set_temperature(1.0)
+        lat.init_spins(1, 50)
+        lat.kmc_setup(fp64=True)
+        w = lat.kmc_run(0.0, 1e-4)  # warm-up: one short pass (tree build, first kernels)
+        t0 = time.perf_counter()
+        st = lat.kmc_run(w["time"], w["time"] + tend)
+        wall = time.perf_counter() - t0
+        ev = st["naccept"] - w["naccept"]
+        lat.close()
+        res[name] = {"workload": f"2048^2 sq/8n potts Q=50 kT 1, tree KMC, 4 sectors, processors "
+                                 f"{procs[0]}x{procs[1]}, FP64 propensities, t += {tend}",
+                     "value": ev / wall, "unit": "events/s", "events": ev, "passes": st["npass"],
+                     "roofline": {"bound": "latency", "frac": None,
+                                  "note": "a chain of dependent events per sector; the HBM fraction is not meaningful"}}
+    lat = sg.Lattice("sq/8n", 2048, 2048, 1, "potts", 50, spin_bytes=4, nsector=4, procs=(32, 32, 1), seed=SEED)
+    lat.set_temperature(1.0)
+    lat.init_spins(1, 50)
+    lat.kmc_setup(fp64=False)
+    st = lat.kmc_run(0.0, 0.2)
+    lat.close()
+    res["C3_grid"]["fp32_propensities"] = {"prop_rel_err": st["prop_rel_err"], "dt_rel_err": st["dt_rel_err"],
+                                           "events": st["naccept"], "t": st["time"],
+                                           "against": "all-FP64 propensities of the same chains"}
+    return res
 
 
 def kernel_case(name):

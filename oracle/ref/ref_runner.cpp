@@ -13,11 +13,14 @@
      #! snap TAG        print the hash and all site values
      #! energy          print spparks_energy (only after a run)
      #! timed TAG CMD   run the input command CMD and print its wall time
+     #! appstats        print the app's stats line (App::stats: time,
+                        Naccept, Nreject, Nsweeps)
    Output lines:
      sweep N NACCEPT NATTEMPT HASH TIME
      snap TAG HASH NLOCAL v1 v2 ...
      energy E
      timed TAG SECONDS
+     appstats TIME NACCEPT NREJECT NSWEEPS
 */
 
 #include <cstdio>
@@ -28,7 +31,9 @@
 #include <stdint.h>
 #include <time.h>
 
+#include "app.h"
 #include "library.h"
+#include "spparks.h"
 #include "../philox_oracle.h"
 
 #ifdef SPK_SHIM
@@ -116,6 +121,11 @@ int main(int argc, char **argv) {
         clock_gettime(CLOCK_MONOTONIC, &t1);
         flush_records();
         printf("timed %s %.9f\n", a1, (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec));
+        fflush(stdout);
+      } else if (!strcmp(cmd, "appstats")) {
+        char buf[512];
+        ((SPPARKS_NS::SPPARKS *)spk)->app->stats(buf);
+        printf("appstats %s\n", buf);
         fflush(stdout);
       } else if (!strcmp(cmd, "record")) {
 #ifdef SPK_SHIM
