@@ -664,7 +664,25 @@ def measure_configs(sg, peak, peak_kind):
                                        "roofline": _roofline(r8, 2.0, peak, peak_kind),
                                        "kernel": "per-colour phase kernel, int8"},
                  "packed_over_int8": rp / r8}
-    for name, procs, tend in (("C3_serial", (1, 1, 1), 0.01), ("C3_grid", (32, 32, 1), 1.0)):
+    res.update(measure_configs_c3(sg))
+    lat = sg.Lattice("sq/8n", 2048, 2048, 1, "potts", 50, spin_bytes=4, nsector=4, procs=(32, 32, 1), seed=SEED)
+    lat.set_temperature(1.0)
+    lat.init_spins(1, 50)
+    lat.kmc_setup(fp64=False)
+    st = lat.kmc_run(0.0, 0.2)
+    lat.close()
+    res["C3_grid"]["fp32_propensities"] = {"prop_rel_err": st["prop_rel_err"], "dt_rel_err": st["dt_rel_err"],
+                                           "events": st["naccept"], "t": st["time"],
+                                           "against": "all-FP64 propensities of the same chains"}
+    return res
+
+
+def measure_configs_c3(sg, serial_t=0.02):
+    """Tree KMC on 2048^2 sq/8n Potts Q=50: serial (the configuration as
+    written) and on a 32x32 processor grid, events/s (host clock around a
+    synchronous run, after a short warm-up pass)."""
+    res = {}
+    for name, procs, tend in (("C3_serial", (1, 1, 1), serial_t), ("C3_grid", (32, 32, 1), 1.0)):
         lat = sg.Lattice("sq/8n", 2048, 2048, 1, "potts", 50, spin_bytes=4, nsector=4, procs=procs, seed=SEED)
         lat.set_temperature(1.0)
         lat.init_spins(1, 50)
@@ -680,15 +698,6 @@ def measure_configs(sg, peak, peak_kind):
                      "value": ev / wall, "unit": "events/s", "events": ev, "passes": st["npass"],
                      "roofline": {"bound": "latency", "frac": None,
                                   "note": "a chain of dependent events per sector; the HBM fraction is not meaningful"}}
-    lat = sg.Lattice("sq/8n", 2048, 2048, 1, "potts", 50, spin_bytes=4, nsector=4, procs=(32, 32, 1), seed=SEED)
-    lat.set_temperature(1.0)
-    lat.init_spins(1, 50)
-    lat.kmc_setup(fp64=False)
-    st = lat.kmc_run(0.0, 0.2)
-    lat.close()
-    res["C3_grid"]["fp32_propensities"] = {"prop_rel_err": st["prop_rel_err"], "dt_rel_err": st["dt_rel_err"],
-                                           "events": st["naccept"], "t": st["time"],
-                                           "against": "all-FP64 propensities of the same chains"}
     return res
 
 
@@ -741,6 +750,16 @@ def kernel_case(name):
             ms = lat.timed_sweeps(nsw)
             print(f"{label}: {ms / nsw:.4f} ms per sweep, {lat.n * nsw / (ms * 1e-3):.3e} site-updates/s", flush=True)
             lat.close()
+    elif name == "c3":  # events/s of tree KMC on the 2048^2 configuration, serial and on the 32x32 grid
+        res = measure_configs_c3(sg)
+        for k, v in res.items():
+            print(k, f"{v['value']:.4g} events/s", v["events"], "events", v["passes"], "passes", flush=True)
+    elif name == "kmc_serial":  # tree KMC Potts Q=50 sq/8n 1024^2, one processor, 4 sectors, a short run
+        lat = sg.Lattice("sq/8n", 1024, 1024, 1, "potts", 50, spin_bytes=4, nsector=4, seed=5)
+        lat.set_temperature(1.0)
+        lat.init_spins(1, 50)
+        lat.kmc_setup(fp64=True)
+        print("kmc_serial", lat.kmc_run(0.0, 0.005))
     elif name == "kmc":  # tree KMC Potts Q=50 sq/8n 1024^2, 32x32 processor grid, 4 sectors
         lat = sg.Lattice("sq/8n", 1024, 1024, 1, "potts", 50, spin_bytes=4, nsector=4, procs=(32, 32, 1), seed=5)
         lat.set_temperature(1.0)
@@ -758,7 +777,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--kernel-case", choices=["ensemble", "fused", "rows", "packed", "kmc", "rates"],
+    ap.add_argument("--kernel-case", choices=["ensemble", "fused", "rows", "packed", "kmc", "kmc_serial", "rates", "c3"],
                     help="run one small profiling workload instead of the benchmark")
     args = ap.parse_args()
     if args.kernel_case:

@@ -67,6 +67,7 @@ struct KmcArgs {
   double dt_kmc;
   int fp64;
   int smem_trees;               // 1: the event kernel copies trees to shared memory
+  const int32_t *c_box;         // chain c's box: x0, y0, z0, wx, wy, wz (6 per chain)
 };
 
 template <int LAT>
@@ -377,6 +378,435 @@ __global__ void __launch_bounds__(32) kmc_event_kernel(KmcArgs a, int iset) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Event loop with the tree in shared memory.
+//
+// The same events as kmc_event_kernel, with the memory round trips of an
+// event cut from about forty dependent global loads to two:
+//   * the top 14 levels of the chain's tree (16383 nodes, 128 KB) live in
+//     shared memory for the whole sector phase (the whole tree when it has
+//     at most 14 levels) and are written back at the end;
+//   * below them, the descendants of the level-13 node the pick's walk
+//     reaches (levels 14..D, a "slot") are fetched in one round trip; for
+//     the changed leaves, each lane fetches its leaf's path below level 14
+//     and the path's siblings (all that re-adding the path reads), together
+//     with the site values the event reads;
+//   * a site's chain and leaf index come from its coordinates: a chain is a
+//     box (a processor sub-domain's sector half along each axis) and its
+//     leaves follow ascending site order, so the leaf of (x, y, z) is its
+//     rank in the box (AppLattice::create_set, src/app_lattice.cpp:954-1070);
+//   * the site values within two steps of the event site (every value the
+//     event and the 1 + NN propensities read) are fetched at once into
+//     shared memory.
+// Node values stay bit-identical: each changed leaf's ancestors are re-added
+// as parent = left + right bottom-up (src/solve_tree.cpp:174-200), in shared
+// memory, and written through to the global tree below level 14.
+// Slot layout: a node n at depth j >= 1 below the level-13 node A sits at
+// t = n - (A << j) - 1 (depth j holds 2^j nodes from t = 2^j - 2).
+
+constexpr int kTopLevels = 14;
+constexpr int kTopNodes = (1 << kTopLevels) - 1;  // levels 0..13
+
+// shared memory (bytes) of kmc_tree_event_kernel for a tree of ntotal nodes
+// on a lattice of NN neighbours and dim dimensions; 0 if it does not fit
+inline size_t kmc_tree_smem_bytes(int ntotal, int nn, bool k3d, size_t limit) {
+  const int blk = k3d ? 125 : 25;
+  size_t top, slots = 0;
+  if (ntotal <= kTopNodes) {
+    top = (size_t)ntotal;
+  } else {
+    int nround = (ntotal + 1) / 2, depth = 0;
+    while ((1 << depth) < nround) depth++;
+    const int hb = depth - (kTopLevels - 1);
+    top = (size_t)kTopNodes;
+    slots = (size_t)(nn + 2) * (size_t)((2 << hb) - 2);
+  }
+  const size_t bytes = (top + slots) * 8 + (size_t)blk * 4;
+  return bytes <= limit ? bytes : 0;
+}
+
+// 8-byte asynchronous copy global -> shared (no register round trip, so a
+// lane's copies all fly at once); completed by cp_async_wait_all
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// issue the copy of the descendants of the level-13 node A (depths 1..hb)
+// from the global tree G into slot S, all lanes
+__device__ __forceinline__ void load_slot(const double *G, double *S, int A, int slotn, int lane) {
+  for (int t = lane; t < slotn; t += 32) {
+    const int j = 31 - __clz(t + 2);
+    cp_async8(S + t, G + ((int64_t)A << j) + t + 1);
+  }
+}
+
+template <typename S, int LAT, int APP>
+__global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset) {
+  using St = Stencil<LAT>;
+  constexpr int NN = St::NN;
+  constexpr int BW = 5;                             // block edge: offsets -2..2
+  constexpr int BLK = St::k3d ? BW * BW * BW : BW * BW;
+  constexpr int NQ = (BLK + 31) / 32;               // block entries per lane
+  constexpr int CTR = St::k3d ? 62 : 12;            // block index of offset (0,0,0)
+  constexpr int NSLOT = NN + 2;                     // one per changed leaf, one for the pick
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  extern __shared__ double kmc_smem[];
+  const int lane = threadIdx.x;
+  const int c = blockIdx.x * a.nsector + iset;
+  S *spin = (S *)a.spin;
+  double *G = a.trees + a.c_tree_off[c];
+  const int leaf0 = a.c_leaf0[c];
+  const int ntotal = a.c_ntotal[c];
+  const int depth = 31 - __clz(leaf0 + 1);          // leaves at level depth
+  const bool whole = ntotal <= kTopNodes;
+  const int ntop = whole ? ntotal : kTopNodes;
+  const int hb = whole ? 0 : depth - (kTopLevels - 1);  // leaf depth below a level-13 node
+  const int slotn = whole ? 0 : (2 << hb) - 2;
+  double *top = kmc_smem;
+  double *slots = top + ntop;
+  int *blk = (int *)(slots + (size_t)NSLOT * slotn);
+  const int *box = a.c_box + 6 * c;
+  const int bx = box[0], by = box[1], bz = box[2], wx = box[3], wy = box[4], wz = box[5];
+  // power-of-two box sides: a rank's coordinates by shifts and masks
+  const bool pow2 = ((wx & (wx - 1)) == 0) && ((wy & (wy - 1)) == 0);
+  const int lwx = __ffs(wx) - 1, lwy = __ffs(wy) - 1;
+
+  for (int p = lane; p < ntop; p += 32) cp_async8(top + p, G + p);
+  // this lane's changed site: 0 = the event site, j = neighbour j-1
+  int odx = 0, ody = 0, odz = 0;
+  if (lane >= 1 && lane <= NN) St::offset(lane - 1, odx, ody, odz);
+  const int my_bo = odx + BW * ody + BW * BW * odz;  // its block offset from the centre
+  // this lane's block entries t = lane + 32 q as offsets from the centre
+  int bdx[NQ], bdy[NQ], bdz[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int t = lane + 32 * q;
+    bdx[q] = t % BW - 2;
+    bdy[q] = (t / BW) % BW - 2;
+    bdz[q] = St::k3d ? t / (BW * BW) - 2 : 0;
+  }
+  cp_async_wait_all();
+  __syncwarp();
+
+  int nactive = a.c_nactive[c];
+  unsigned long long k = a.c_events[c];
+  double sum = top[0];
+  if (lane == 0 && nactive > 0) {
+    double ptmp = sum / nactive;
+    atomicMax(a.pmax_bits, (unsigned long long)__double_as_longlong(ptmp));
+  }
+  double timesector = 0.0;
+  unsigned int done_events = 0;
+  double pre_ux = 0.0, pre_uz = 0.0, pre_log = 0.0;
+  int pre_left = 0;
+  while (__double_as_longlong(sum) != 0) {  // sum >= 0
+    if (pre_left == 0) {
+      const U4 pw = kmc_block(a.seed, (uint32_t)c, k + (unsigned long long)lane);
+      pre_ux = word_to_uniform(pw.x);
+      pre_uz = word_to_uniform(pw.z);
+      pre_log = log(word_to_uniform(pw.y));
+      pre_left = 32;
+    }
+    const int slot_no = 32 - pre_left;
+    pre_left--;
+    const double ux = __shfl_sync(FULL, pre_ux, slot_no);
+    const double uz = __shfl_sync(FULL, pre_uz, slot_no);
+    const double lu = __shfl_sync(FULL, pre_log, slot_no);
+    k++;
+    // the clock step does not depend on the pick (SolveTree::event,
+    // src/solve_tree.cpp:130-143)
+    const double dt = -1.0 / sum * lu;
+    // SolveTree::find through the cached levels (src/solve_tree.cpp:207-224)
+    int node = 0;
+    double value = ux * sum;
+    if (lane == 0) {
+      const int stop = whole ? leaf0 : (kTopNodes >> 1);  // children of nodes below it are cached
+      while (node < stop) {
+        const int left = 2 * node + 1;
+        const double tl = top[left];
+        if (nonneg_le(value, tl)) node = left;
+        else {
+          value -= tl;
+          node = left + 1;
+        }
+      }
+    }
+    node = __shfl_sync(FULL, node, 0);
+    double *SF = slots + (size_t)(NSLOT - 1) * slotn;  // the pick's slot
+    if (!whole) {
+      // node is the level-13 node A: its descendants in one round trip
+      load_slot(G, SF, node, slotn, lane);
+      cp_async_wait_all();
+      __syncwarp();
+      if (lane == 0) {
+        const int A = node;
+        for (int j = 0; j < hb; j++) {
+          const int left = 2 * node + 1;
+          const double tl = SF[left - (A << (j + 1)) - 1];
+          if (nonneg_le(value, tl)) node = left;
+          else {
+            value -= tl;
+            node = left + 1;
+          }
+        }
+      }
+      node = __shfl_sync(FULL, node, 0);
+    }
+    const int m = node - leaf0;
+    timesector += dt;
+    if (nonneg_le(a.dt_kmc, timesector)) break;  // timesector >= dt_kmc
+    const int pA = whole ? 0 : ((node + 1) >> hb) - 1;  // the pick's level-13 node
+    // the site of leaf m: its rank in the chain's box
+    int x, y, z;
+    if (pow2) {
+      x = bx + (m & (wx - 1));
+      y = by + ((m >> lwx) & (wy - 1));
+      z = bz + (m >> (lwx + lwy));
+    } else {
+      x = bx + m % wx;
+      const int r = m / wx;
+      y = by + r % wy;
+      z = bz + r / wy;
+    }
+    const int64_t i = (int64_t)x + (int64_t)a.nx * ((int64_t)y + (int64_t)a.ny * z);
+    // site values within two steps (wrapped): loads first, stores after
+    int64_t bidx[NQ];
+    int bval[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      bidx[q] = -1;
+      if (lane + 32 * q < BLK) {
+        bidx[q] = wrap_index<LAT>(x, y, z, bdx[q], bdy[q], bdz[q], a.nx, a.ny, a.nz);
+        bval[q] = (int)spin[bidx[q]];
+      }
+    }
+    // this lane's changed site: in the chain? its leaf, and its level-13 node
+    bool mine = false;
+    int leaf = -1, A = -1;
+    if (lane <= NN) {
+      int xs = x + odx, ys = y + ody, zs = z + odz;
+      xs = xs < 0 ? xs + a.nx : (xs >= a.nx ? xs - a.nx : xs);
+      ys = ys < 0 ? ys + a.ny : (ys >= a.ny ? ys - a.ny : ys);
+      if (St::k3d) zs = zs < 0 ? zs + a.nz : (zs >= a.nz ? zs - a.nz : zs);
+      else zs = 0;
+      const unsigned ux_ = (unsigned)(xs - bx), uy_ = (unsigned)(ys - by), uz_ = (unsigned)(zs - bz);
+      if (ux_ < (unsigned)wx && uy_ < (unsigned)wy && uz_ < (unsigned)wz) {
+        mine = true;
+        leaf = (int)((uz_ * (unsigned)wy + uy_) * (unsigned)wx + ux_);
+        A = whole ? 0 : ((leaf0 + leaf + 1) >> hb) - 1;
+      }
+    }
+    const int lnode = leaf0 + leaf;
+    // one slot per distinct level-13 node, held by its lowest lane; each
+    // lane fetches its own path below that node and the path's siblings
+    // while the event is picked
+    double *MS = slots;
+    if (!whole) {
+      const unsigned grp = __match_any_sync(FULL, mine ? A : -1);
+      const int sl = mine ? __ffs(grp) - 1 : 0;  // a lane <= NN
+      MS = slots + (size_t)sl * slotn;
+      if (mine) {
+        int nd = lnode;
+        for (int j = hb; j >= 1; j--) {
+          const int sib = (nd & 1) ? nd + 1 : nd - 1;
+          cp_async8(MS + (nd - (A << j) - 1), G + nd);
+          cp_async8(MS + (sib - (A << j) - 1), G + sib);
+          nd = (nd - 1) >> 1;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+      if (bidx[q] >= 0) blk[lane + 32 * q] = bval[q];
+    __syncwarp();
+    // site_event (src/app_potts.cpp:196-244, src/app_ising.cpp:170-196):
+    // lane j < NN computes the weight of neighbour j's value; the running
+    // sum then takes the first appearances of values other than the site's
+    // own in neighbour order, as the reference adds them, and stops at the
+    // first that reaches the threshold
+    int newv = 0;
+    {
+      const int own = blk[CTR];
+      if (APP == SPKGPU_ISING) {
+        newv = own == 1 ? 2 : 1;
+      } else {
+        int nb[NN];
+#pragma unroll
+        for (int j = 0; j < NN; j++) {
+          int dx, dy, dz;
+          St::offset(j, dx, dy, dz);
+          nb[j] = blk[CTR + dx + BW * dy + BW * BW * dz];
+        }
+        const double pm = whole ? top[node] : SF[node - (pA << hb) - 1];
+        const double threshhold = uz * pm;
+        const int e0 = count_unlike<NN>(own, nb);
+        const uint32_t first = first_appearance<NN>(own, nb);
+        const int mv = lane < NN ? pick_value<NN>(nb, lane) : own;
+        const int e1 = count_unlike<NN>(mv, nb);
+        const bool live = lane < NN && ((first >> lane) & 1u);
+        int val = own;
+        bool found = false;
+        if (a.fp64) {
+          const double term = !live ? 0.0 : (e1 <= e0 ? 1.0 : (a.zero_t ? 0.0 : a.pexp[e1 - e0]));
+          double prob = 0.0;
+#pragma unroll
+          for (int j = 0; j < NN; j++) {
+            const double tj = __shfl_sync(FULL, term, j);
+            if (!found && ((first >> j) & 1u)) {
+              prob += tj;
+              val = nb[j];
+              found = nonneg_le(threshhold, prob);  // prob >= threshhold
+            }
+          }
+        } else {
+          const float term = !live ? 0.0f : (e1 <= e0 ? 1.0f : (a.zero_t ? 0.0f : a.pexpf[e1 - e0]));
+          float prob = 0.0f;
+#pragma unroll
+          for (int j = 0; j < NN; j++) {
+            const float tj = __shfl_sync(FULL, term, j);
+            if (!found && ((first >> j) & 1u)) {
+              prob += tj;
+              val = nb[j];
+              found = nonneg_le(threshhold, (double)prob);
+            }
+          }
+        }
+        newv = val;
+      }
+      if (lane == 0) spin[i] = (S)newv;
+    }
+    // every block entry holding site i (more than one on periodic extents < 5)
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+      if (bidx[q] == i) blk[lane + 32 * q] = newv;
+    cp_async_wait_all();
+    __syncwarp();
+    // the propensity of this lane's site from the block
+    double p = 0.0;
+    if (mine) {
+      const int cb = CTR + my_bo;
+      const int own = blk[cb];
+      int nb[NN];
+#pragma unroll
+      for (int j = 0; j < NN; j++) {
+        int dx, dy, dz;
+        St::offset(j, dx, dy, dz);
+        nb[j] = blk[cb + dx + BW * dy + BW * BW * dz];
+      }
+      const int e0 = count_unlike<NN>(own, nb);
+      if (APP == SPKGPU_ISING) {
+        const int e1 = count_unlike<NN>(own == 1 ? 2 : 1, nb);
+        p = e1 <= e0 ? 1.0 : (a.zero_t ? 0.0 : (a.fp64 ? a.pexp[e1 - e0] : (double)a.pexpf[e1 - e0]));
+      } else {
+        const uint32_t first = first_appearance<NN>(own, nb);
+        if (a.fp64) {
+#pragma unroll
+          for (int j = 0; j < NN; j++) {
+            if (!((first >> j) & 1u)) continue;
+            const int e1 = count_unlike<NN>(nb[j], nb);
+            if (e1 <= e0) p += 1.0;
+            else if (!a.zero_t) p += a.pexp[e1 - e0];
+          }
+        } else {
+          float pf = 0.0f;
+#pragma unroll
+          for (int j = 0; j < NN; j++) {
+            if (!((first >> j) & 1u)) continue;
+            const int e1 = count_unlike<NN>(nb[j], nb);
+            if (e1 <= e0) pf += 1.0f;
+            else if (!a.zero_t) pf += a.pexpf[e1 - e0];
+          }
+          p = (double)pf;
+        }
+      }
+    }
+    // the leaves (a leaf reached by several lanes is set once: the values
+    // agree), num_active as SolveTree::set counts it
+    const unsigned lgrp = __match_any_sync(FULL, mine ? leaf : -1);
+    const bool setter = mine && (__ffs(lgrp) - 1) == lane;
+    int dact = 0;
+    if (setter) {
+      double *lp = whole ? &top[lnode] : &MS[lnode - (A << hb) - 1];
+      dact = (__double_as_longlong(p) != 0) - (__double_as_longlong(*lp) != 0);
+      *lp = p;
+      if (!whole) G[lnode] = p;
+    }
+    nactive += __reduce_add_sync(FULL, dact);
+    __syncwarp();
+    // ancestors: below level 14 in the slots (written through to G), then
+    // the cached levels; lanes on a shared path write equal values
+    int nd = lnode;
+    if (!whole) {
+      for (int j = hb - 1; j >= 1; j--) {
+        if (mine) {
+          nd = (nd - 1) >> 1;
+          const int tl = 2 * nd + 1 - (A << (j + 1)) - 1;
+          const double v = MS[tl] + MS[tl + 1];
+          MS[nd - (A << j) - 1] = v;
+          G[nd] = v;
+        }
+        __syncwarp();
+      }
+      if (mine) {
+        nd = A;
+        top[A] = MS[0] + MS[1];
+      }
+      __syncwarp();
+    }
+    // cached levels: in step up to the lowest common ancestor of the changed
+    // leaves (kmerge levels above the leaves), then lane 0 (whose path every
+    // other path has joined) alone, with the siblings fetched first
+    const unsigned lmin = __reduce_min_sync(FULL, mine ? (unsigned)leaf : 0xFFFFFFFFu);
+    const unsigned lmax = __reduce_max_sync(FULL, mine ? (unsigned)leaf : 0u);
+    const int kmerge = lmin == lmax ? 0 : 32 - __clz(lmin ^ lmax);
+    const int steps = whole ? kmerge : max(0, kmerge - hb);
+    for (int q = 0; q < steps; q++) {
+      if (mine) {
+        nd = (nd - 1) >> 1;
+        top[nd] = top[2 * nd + 1] + top[2 * nd + 2];
+      }
+      __syncwarp();
+    }
+    double root = 0.0;
+    if (lane == 0) {
+      double v = top[nd];
+      const int lev = 31 - __clz(nd + 1);  // levels above nd
+      double sv[kTopLevels];
+      int sn = nd;
+#pragma unroll
+      for (int q = 0; q < kTopLevels; q++) {
+        if (q < lev) {
+          sv[q] = top[(sn & 1) ? sn + 1 : sn - 1];
+          sn = (sn - 1) >> 1;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kTopLevels; q++) {
+        if (q < lev) {
+          const bool left = nd & 1;
+          nd = (nd - 1) >> 1;
+          v = left ? v + sv[q] : sv[q] + v;
+          top[nd] = v;
+        }
+      }
+      root = v;
+    }
+    sum = __shfl_sync(FULL, root, 0);
+    __syncwarp();
+    done_events++;
+  }
+  __syncwarp();
+  for (int p = lane; p < ntop; p += 32) G[p] = top[p];
+  if (lane == 0) {
+    a.c_events[c] = k;
+    a.c_nactive[c] = nactive;
+    if (done_events) atomicAdd(a.naccept, (unsigned long long)done_events);
+  }
+}
+
 }  // namespace spk
 
 using namespace spk;
@@ -394,6 +824,9 @@ struct KmcState {
   int max_ntotal = 0;
   std::vector<int64_t> border_off;  // per sector: offset into border list (nsector+1)
   int32_t *d_setof = nullptr, *d_i2site = nullptr, *d_site2i = nullptr, *d_border = nullptr;
+  int32_t *d_box = nullptr;         // chain boxes (6 per chain)
+  bool boxes = false;               // every chain is a box in ascending site order
+  size_t tree_smem = 0;             // shared memory of kmc_tree_event_kernel (0: global-tree kernel)
   int64_t *d_site_off = nullptr, *d_tree_off = nullptr;
   int32_t *d_nloc = nullptr, *d_leaf0 = nullptr, *d_ntotal = nullptr, *d_nactive = nullptr;
   unsigned long long *d_events = nullptr;
@@ -414,6 +847,7 @@ void spk_kmc_free(spkgpu_lattice *h) {
   cudaFree(k->d_i2site);
   cudaFree(k->d_site2i);
   cudaFree(k->d_border);
+  cudaFree(k->d_box);
   cudaFree(k->d_site_off);
   cudaFree(k->d_tree_off);
   cudaFree(k->d_nloc);
@@ -467,6 +901,7 @@ static KmcArgs kmc_args(spkgpu_lattice *h) {
   a.dt_kmc = k->dt_kmc;
   a.fp64 = k->fp64;
   a.smem_trees = ((size_t)k->max_ntotal * 8 <= 48 * 1024) ? 1 : 0;
+  a.c_box = k->d_box;
   return a;
 }
 
@@ -491,7 +926,17 @@ static cudaError_t launch_sum64_t(int app, const KmcArgs &a, double *chain_sum, 
 }
 
 template <typename S, int LAT>
-static cudaError_t launch_events_t(int app, const KmcArgs &a, int iset, int nprocs, size_t smem, cudaStream_t s) {
+static cudaError_t launch_events_t(int app, const KmcArgs &a, int iset, int nprocs, size_t smem, size_t tree_smem,
+                                   cudaStream_t s) {
+  if (tree_smem) {
+    auto f = app == SPKGPU_ISING ? kmc_tree_event_kernel<S, LAT, SPKGPU_ISING> : kmc_tree_event_kernel<S, LAT, SPKGPU_POTTS>;
+    if (tree_smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem);
+      if (e != cudaSuccess) return e;
+    }
+    f<<<nprocs, 32, tree_smem, s>>>(a, iset);
+    return cudaGetLastError();
+  }
   if (app == SPKGPU_ISING) {
     auto f = kmc_event_kernel<S, LAT, SPKGPU_ISING>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -506,11 +951,11 @@ static cudaError_t launch_events_t(int app, const KmcArgs &a, int iset, int npro
 
 template <typename S>
 static cudaError_t dispatch_lat(int lattice, int app, int what, const KmcArgs &a, const int32_t *list, int64_t n,
-                                int iset, int nprocs, size_t smem, cudaStream_t s, int sms) {
+                                int iset, int nprocs, size_t smem, size_t tree_smem, cudaStream_t s, int sms) {
 #define SPK_KMC_CASE(LATV)                                                                   \
   case LATV:                                                                                 \
     return what == 0 ? launch_prop_t<S, LATV>(app, a, list, n, s, sms)                       \
-                     : launch_events_t<S, LATV>(app, a, iset, nprocs, smem, s);
+                     : launch_events_t<S, LATV>(app, a, iset, nprocs, smem, tree_smem, s);
   switch (lattice) {
     SPK_KMC_CASE(SPKGPU_SQ_4N)
     SPK_KMC_CASE(SPKGPU_SQ_8N)
@@ -588,10 +1033,11 @@ static cudaError_t kmc_launch(spkgpu_lattice *h, int what, const KmcArgs &a, con
   int nprocs = k->nchains / h->d.nsector;
   size_t smem = a.smem_trees ? (size_t)k->max_ntotal * 8 : 0;
   h->launches++;
+  const size_t ts = k->tree_smem;
   switch (h->spin_bytes) {
-    case 1: return dispatch_lat<int8_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, h->stream, h->num_sms);
-    case 2: return dispatch_lat<int16_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, h->stream, h->num_sms);
-    case 4: return dispatch_lat<int32_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, h->stream, h->num_sms);
+    case 1: return dispatch_lat<int8_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, ts, h->stream, h->num_sms);
+    case 2: return dispatch_lat<int16_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, ts, h->stream, h->num_sms);
+    case 4: return dispatch_lat<int32_t>(h->d.lattice, h->d.app, what, a, list, n, iset, nprocs, smem, ts, h->stream, h->num_sms);
   }
   return cudaErrorInvalidValue;
 }
@@ -655,6 +1101,34 @@ extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, 
   }
   std::vector<int32_t> site2i(n);
   for (int64_t i = 0; i < n; i++) site2i[site_off[setof[i]] + i2site[i]] = (int32_t)i;
+  // chain boxes: along each axis a chain takes the coordinates of its
+  // processor (and of its sector half where the sectors split that axis);
+  // each must be one run of coordinates and the box must hold the chain
+  std::vector<int32_t> box((size_t)k->nchains * 6);
+  k->boxes = true;
+  {
+    const int split[3] = {1, nsec >= 4 ? 1 : 0, nsec == 8 ? 1 : 0};
+    for (int c = 0; c < k->nchains && k->boxes; c++) {
+      const int proc = c / nsec, msec = c % nsec;
+      const int pc[3] = {proc % d.procs[0], (proc / d.procs[0]) % d.procs[1], proc / (d.procs[0] * d.procs[1])};
+      const int hc[3] = {msec & 1, (msec >> 1) & 1, (msec >> 2) & 1};
+      int64_t vol = 1;
+      for (int ax = 0; ax < 3; ax++) {
+        int lo = -1, hi = -2, cnt = 0;
+        for (int v = 0; v < dims[ax]; v++) {
+          if (blob_proc[ax][v] != pc[ax] || (split[ax] && blob_half[ax][v] != hc[ax])) continue;
+          if (lo < 0) lo = v;
+          hi = v;
+          cnt++;
+        }
+        if (cnt == 0 || cnt != hi - lo + 1) k->boxes = false;
+        box[6 * c + ax] = lo;
+        box[6 * c + 3 + ax] = cnt;
+        vol *= cnt;
+      }
+      if (vol != nloc[c]) k->boxes = false;
+    }
+  }
   // border sites (a neighbour in another chain), grouped by sector index in
   // the order chains of that sector appear (find_border_sites,
   // src/app_lattice.cpp:1094-1149)
@@ -697,7 +1171,7 @@ extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, 
       !dm((void **)&k->d_leaf0, k->nchains * 4) || !dm((void **)&k->d_ntotal, k->nchains * 4) ||
       !dm((void **)&k->d_nactive, k->nchains * 4) || !dm((void **)&k->d_events, k->nchains * 8) ||
       !dm((void **)&k->d_trees, tree_off[k->nchains] * 8) || !dm((void **)&k->d_scalars, 4 * 8) ||
-      !dm((void **)&k->d_sum64, k->nchains * 8)) {
+      !dm((void **)&k->d_sum64, k->nchains * 8) || !dm((void **)&k->d_box, box.size() * 4)) {
     spk_kmc_free(h);
     return spk_fail(h, SPKGPU_ERR_NOMEM, "KMC allocation failed");
   }
@@ -710,6 +1184,16 @@ extern "C" int spkgpu_kmc_setup(spkgpu_lattice *h, int32_t adapt, double nstop, 
   KMC_CUDA(h, cudaMemcpy(k->d_nloc, nloc.data(), k->nchains * 4, cudaMemcpyHostToDevice));
   KMC_CUDA(h, cudaMemcpy(k->d_leaf0, leaf0.data(), k->nchains * 4, cudaMemcpyHostToDevice));
   KMC_CUDA(h, cudaMemcpy(k->d_ntotal, ntotal.data(), k->nchains * 4, cudaMemcpyHostToDevice));
+  KMC_CUDA(h, cudaMemcpy(k->d_box, box.data(), box.size() * 4, cudaMemcpyHostToDevice));
+  // the shared-memory tree kernel where the chains are boxes and the tree
+  // fits; the global-tree kernel otherwise
+  k->tree_smem = 0;
+  if (k->boxes) {
+    int optin = 0;
+    KMC_CUDA(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->d.device));
+    k->tree_smem = kmc_tree_smem_bytes(k->max_ntotal, nn, d.lattice == SPKGPU_SC_6N || d.lattice == SPKGPU_SC_26N,
+                                       (size_t)optin);
+  }
   KMC_CUDA(h, cudaMemset(k->d_events, 0, k->nchains * 8));
   KMC_CUDA(h, cudaMemset(k->d_trees, 0, tree_off[k->nchains] * 8));
   KMC_CUDA(h, cudaMemset(k->d_scalars, 0, 4 * 8));
