@@ -17,6 +17,7 @@
 
 #include <cuda/atomic>
 #include <cuda_runtime.h>
+#include <stdio.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -76,6 +77,8 @@ struct EnsArgs {
   const int32_t *pair_rep;      // warp form: replica of each CTA's tile pair
   const int32_t *pair_tile;     // warp form: the pair's two tiles (-1: none)
   int npairs;
+  long long spin_limit;         // grid barrier: waits before giving up
+  int skip_block;               // grid barrier: this CTA never arrives (error-path test), -1 none
 };
 
 constexpr long long kBarrierSpinLimit = 1LL << 25;  // ~seconds with nanosleep: then give up
@@ -85,7 +88,10 @@ constexpr long long kBarrierSpinLimit = 1LL << 25;  // ~seconds with nanosleep: 
 // Arrival is a release RMW and the wait an acquire load at device scope, so
 // the writes of every block before the barrier (spins, temperatures) are
 // visible to every block after it.
-__device__ bool grid_barrier(EnsCtl *ctl) {
+// A CTA whose index is `skip` (the error-path test; -1 in every normal run)
+// neither arrives nor waits: the others give up after `limit` waits.
+__device__ bool grid_barrier(EnsCtl *ctl, long long limit, int skip) {
+  if ((int)blockIdx.x == skip) return false;
   __syncthreads();
   if (threadIdx.x == 0) {
     cuda::atomic_ref<unsigned int, cuda::thread_scope_device> gen(ctl->bar_gen);
@@ -99,7 +105,7 @@ __device__ bool grid_barrier(EnsCtl *ctl) {
     } else {
       long long it = 0;
       while (gen.load(cuda::memory_order_acquire) == my) {
-        if (++it > kBarrierSpinLimit || err.load(cuda::memory_order_relaxed)) {
+        if (++it > limit || err.load(cuda::memory_order_relaxed)) {
           err.store(1, cuda::memory_order_relaxed);
           break;
         }
@@ -293,7 +299,7 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
     }
     cp_async_wait<0>();
     parity ^= 1;
-    ok = grid_barrier(ctl);
+    ok = grid_barrier(ctl, a.spin_limit, a.skip_block);
     if (!ok) break;
     uint32_t done = sweep0 + (uint32_t)s + 1;
     if (a.exchange_every > 0 && done % (uint32_t)a.exchange_every == 0) {
@@ -301,11 +307,11 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
       const S *curbuf = (const S *)(parity ? a.buf1 : a.buf0);
       for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x)
         tile_bonds<S>(a, t, replica_of_tile(a.tile_start, a.nrep, t), curbuf);
-      ok = grid_barrier(ctl);
+      ok = grid_barrier(ctl, a.spin_limit, a.skip_block);
       if (!ok) break;
       if (blockIdx.x == 0) exchange_round(a, xround);
       xround++;
-      ok = grid_barrier(ctl);
+      ok = grid_barrier(ctl, a.spin_limit, a.skip_block);
     }
   }
   unsigned long long w = my_changed;
@@ -317,7 +323,7 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 16 : 12) e
     for (int k = 0; k < kTileThreads / 32; k++) tot += red[k];
     if (tot) atomicAdd(&ctl->naccept, tot);
   }
-  ok = grid_barrier(ctl) && ok;
+  ok = grid_barrier(ctl, a.spin_limit, a.skip_block) && ok;
   if (blockIdx.x == 0 && threadIdx.x == 0 && ok) {
     ctl->parity = parity;
     ctl->sweep = sweep0 + (uint32_t)a.nsweeps;
@@ -999,6 +1005,19 @@ int spkgpu_ensemble_create(const spkgpu_ensemble_desc *desc, spkgpu_ensemble **o
   a.pair_rep = e->d_pair_rep;
   a.pair_tile = e->d_pair_tile;
   a.npairs = e->npairs;
+  a.spin_limit = kBarrierSpinLimit;
+  a.skip_block = -1;
+  // error-path test of the persistent form: SPKGPU_ENSEMBLE_BARRIER_TEST=
+  // "limit,cta" makes the grid barrier give up after `limit` waits and CTA
+  // `cta` skip its arrival, so the bounded wait runs out without a hang
+  if (const char *env = getenv("SPKGPU_ENSEMBLE_BARRIER_TEST")) {
+    long long lim = 0;
+    int cta = -1;
+    if (sscanf(env, "%lld,%d", &lim, &cta) == 2 && lim > 0) {
+      a.spin_limit = lim;
+      a.skip_block = cta;
+    }
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(SPKGPU_ERR_CUDA);
   // pick the faster execution form for this replica set, then start from a
   // clean state and capture one step of it as a graph

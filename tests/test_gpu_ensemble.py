@@ -213,3 +213,35 @@ def test_ensemble_replicas_match_reference_fixtures(sg, ref_fixtures, monkeypatc
                 assert format(oracle.spin_hash(ens.replica(out, r)), "016x") == fx["sweeps"][s][3], (mode, r, s)
         assert ens.stats()["naccept"] == sum(fx["sweeps"][-1][1] for fx in fxs)
         ens.close()
+
+
+def test_persistent_grid_barrier_gives_up_and_reports_a_device_error(sg, monkeypatch):
+    """The persistent form's grid barrier waits a bounded number of times.
+    With SPKGPU_ENSEMBLE_BARRIER_TEST one CTA never arrives and the limit is
+    2000 waits: the other CTAs give up, set the error word and leave, so the
+    run ends on its own and spkgpu_ensemble_synchronize reports
+    SPKGPU_ERR_DEVICE.  The context stays usable: a new ensemble on the same
+    device then gives the oracle's results."""
+    L, T = [64, 96, 128], [1.8, 2.3, 2.9]
+    spins = [oracle.init_spins(90 + r, l * l, 1, 2) for r, l in enumerate(L)]
+    monkeypatch.setenv("SPKGPU_ENSEMBLE_MODE", "persistent")
+    monkeypatch.setenv("SPKGPU_ENSEMBLE_BARRIER_TEST", "2000,1")
+    ens = sg.Ensemble(L, T, "ising", 2, seed=17, exchange_every=2)
+    assert ens.mode()["mode"] == "persistent"
+    ens.upload(np.concatenate(spins))
+    with pytest.raises(sg.SpkGpuError) as ei:
+        ens.run(4)
+        ens.synchronize()
+    assert ei.value.code == -7  # SPKGPU_ERR_DEVICE
+    ens.close()
+    monkeypatch.delenv("SPKGPU_ENSEMBLE_BARRIER_TEST")
+    ens = sg.Ensemble(L, T, "ising", 2, seed=17, exchange_every=2)
+    ens.upload(np.concatenate(spins))
+    ens.run(4)
+    got = ens.download()
+    orc = oracle.EnsembleOracle(L, T, "ising", 2, seed=17, every=2)
+    ref = [x.copy() for x in spins]
+    orc.run(ref, 4)
+    assert all(np.array_equal(ens.replica(got, r), ref[r]) for r in range(len(L)))
+    assert ens.stats()["naccept"] == orc.naccept
+    ens.close()
