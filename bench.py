@@ -652,7 +652,8 @@ def measure_configs(sg, peak, peak_kind):
     res["C0"] = {"workload": "128^2 sq/4n ising int32 kT 2.269, 100 sweeps (the whole job)", "value": r,
                  "unit": UNIT, "ms_per_sweep": ms,
                  "roofline": {**_roofline(r, 8.0, peak, peak_kind, "latency"),
-                              "note": "64 KB lattice, L2-resident: the launch sequence bounds it, not HBM"}}
+                              "note": "64 KB lattice held in one 8-CTA cluster's shared memory for all 100 sweeps "
+                                      "(one launch); two cluster barriers per sweep bound it, not HBM"}}
     r, ms, _ = _sweep_rate(sg, C1, 20, warm=2)
     res["C1"] = {"workload": "256^3 sc/26n potts/neighonly Q=100 int16 kT 0.5, 20 of the 1000 sweeps", "value": r,
                  "unit": UNIT, "ms_per_sweep": ms, "roofline": _roofline(r, 4.0, peak, peak_kind, "alu")}

@@ -84,7 +84,9 @@ typedef struct spkgpu_desc {
   uint32_t seed;        /* Philox key word */
   int32_t device;       /* CUDA device ordinal */
   int32_t variant;      /* 0 = fastest kernel for the configuration,
-                           1 = always the per-colour phase kernel */
+                           1 = always the per-colour phase kernel,
+                           2 = the tile kernel (one launch per sweep) even
+                               where the whole lattice fits one CTA */
 } spkgpu_desc;
 
 typedef struct spkgpu_stats {

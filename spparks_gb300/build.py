@@ -23,6 +23,7 @@ SOURCES = [
     "spkgpu_api.cpp",
     "sweep_generic.cu",
     "sweep_fused2d.cu",
+    "sweep_resident.cu",
     "kmc.cu",
     "ensemble.cu",
     "noalloc.cu",

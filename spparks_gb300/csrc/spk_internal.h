@@ -127,6 +127,13 @@ bool fused2d_supported(int lattice, int app, int spin_bytes, int nx, int ny);
 cudaError_t launch_fused2d(int lattice, int app, int spin_bytes, const FusedArgs &a, cudaStream_t s,
                            int num_sms);
 
+// all sweeps of one call for an sq/4n lattice that fits one CTA's shared
+// memory (sweep_resident.cu); same eligibility as the fused sweep otherwise
+bool resident_supported(int lattice, int app, int spin_bytes, int nx, int ny);
+cudaError_t launch_resident_sweeps(int app, int spin_bytes, void *spin, int nx, int ny, uint32_t seed,
+                                   uint32_t sweep0, int nsweeps, int nspins, unsigned long long *naccept,
+                                   const AcceptTable &acc, cudaStream_t s);
+
 // row-pair sweep for sq/8n and sc/26n without sectors (sweep_rows.cu)
 bool rows_supported(int lattice, int spin_bytes, int nx, int nspins);
 cudaError_t launch_rows_sweep(int lattice, int app, int spin_bytes, void *spin, int nx, int ny, int nz,
@@ -192,6 +199,7 @@ struct spkgpu_lattice {
   int64_t nattempt = 0;
   int64_t launches = 0;
   bool fused_ok = false;         // sq/4n fused tile sweep
+  bool resident_ok = false;      // sq/4n lattice in one CTA's shared memory
   bool rows_ok = false;          // sq/8n, sc/26n row-pair sweep
   std::string err;
   // KMC state (kmc.cu)

@@ -156,7 +156,7 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
     return SPKGPU_ERR_ARG;
   }
   if (d.rng != SPKGPU_RNG_PHILOX && d.rng != SPKGPU_RNG_STRICT) return SPKGPU_ERR_ARG;
-  if (d.variant != 0 && d.variant != 1) return SPKGPU_ERR_ARG;
+  if (d.variant < 0 || d.variant > 2) return SPKGPU_ERR_ARG;
   if (d.rng == SPKGPU_RNG_STRICT && d.nsector > 1) return SPKGPU_ERR_ARG;  // src/app_lattice.cpp:155-156
   // colouring needs even extents (Lattice::ncolors, src/lattice.cpp:187-228)
   if (d.nx % 2 || d.ny % 2 || (!spk::is2d(d.lattice) && d.nz % 2)) return SPKGPU_ERR_ARG;
@@ -239,9 +239,10 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
     return fail(SPKGPU_ERR_CUDA);
   }
   h->axes = ax;
-  h->fused_ok = (!packed && d.variant == 0 && d.nsector == 1 && d.nloop == 1 &&
+  h->fused_ok = (!packed && (d.variant == 0 || d.variant == 2) && d.nsector == 1 && d.nloop == 1 &&
                  d.rng == SPKGPU_RNG_PHILOX && !d.mask &&
                  spk::fused2d_supported(d.lattice, d.app, sb, d.nx, d.ny));
+  h->resident_ok = h->fused_ok && d.variant == 0 && spk::resident_supported(d.lattice, d.app, sb, d.nx, d.ny);
   if (h->fused_ok) {
     if (cudaMalloc(&h->d_spin_alt, (size_t)h->n * sb) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
   }
@@ -422,6 +423,16 @@ static int enqueue_sweeps(spkgpu_lattice *h, int32_t nsweeps) {
   unsigned long long *nacc = h->d_counters + kNacceptSlots;
   bool z3 = !spk::is2d(d.lattice);
   int nsec = d.nsector;
+  if (h->resident_ok && nsweeps > 0) {
+    // every sweep of the call in one launch, in place
+    SPK_CUDA(h, spk::launch_resident_sweeps(d.app, h->spin_bytes, h->d_spin, d.nx, d.ny, d.seed, (uint32_t)h->sweep,
+                                            nsweeps, d.nspins, nacc, h->acc, h->stream));
+    h->launches++;
+    h->sweep += nsweeps;
+    h->nsweeps_done += nsweeps;
+    h->nattempt += h->n * (int64_t)nsweeps;
+    return SPKGPU_OK;
+  }
   for (int32_t s = 0; s < nsweeps; s++) {
     uint32_t sweep = (uint32_t)h->sweep;
     if (h->packed) {

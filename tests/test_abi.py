@@ -51,7 +51,7 @@ def test_version_and_invalid_descriptions(lib):
         dict(lattice=sg.SQ_4N, nsector=8),  # 2d with 8 sectors
         dict(rng=sg.RNG_STRICT, nsector=4),  # color/strict with sectors
         dict(nspins=200, spin_bytes=1),
-        dict(variant=2),
+        dict(variant=3),
     ]
     for b in bad:
         d = sg.Desc()

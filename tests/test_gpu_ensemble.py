@@ -28,7 +28,7 @@ def test_fused_tile_sweep_matches_oracle(sg, app, q, T, nx, ny, sb):
     cfg = oracle.make_cfg("sq/4n", nx, ny, 1, app, q, T, seed=seed)
     ref = spin.copy()
     na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 6)
-    lat = sg.Lattice("sq/4n", nx, ny, 1, app, q, spin_bytes=sb, seed=seed)
+    lat = sg.Lattice("sq/4n", nx, ny, 1, app, q, spin_bytes=sb, seed=seed, variant=2)
     lat.set_temperature(T)
     lat.upload(spin)
     got = []
@@ -40,6 +40,33 @@ def test_fused_tile_sweep_matches_oracle(sg, app, q, T, nx, ny, sb):
     assert (st["naccept"], st["nattempt"]) == (na, nt)
     # the fused path issues one launch per sweep
     assert lat.launch_count() <= 2 + 6 + 6
+
+
+@pytest.mark.parametrize("app,q,T", [("ising", 2, 2.269), ("potts", 20, 0.7), ("potts/neighonly", 9, 0.4),
+                                     ("potts/neigh", 5, 1.1), ("ising", 2, 0.0), ("ising", 2, 1e30)])
+@pytest.mark.parametrize("nx,ny,sb", [(32, 32, 1), (64, 96, 2), (128, 128, 4), (96, 64, 1)])
+def test_resident_sweeps_match_oracle(sg, app, q, T, nx, ny, sb):
+    """sq/4n lattices that fit one CTA's shared memory: every sweep of a
+    call in one launch (calls of 1, 5 and 4 sweeps), equal to the oracle at
+    the end of each call, with the same change and attempt counts"""
+    seed = 4321
+    spin = oracle.init_spins(seed, nx * ny, 1, q)
+    cfg = oracle.make_cfg("sq/4n", nx, ny, 1, app, q, T, seed=seed)
+    ref = spin.copy()
+    na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 10)
+    lat = sg.Lattice("sq/4n", nx, ny, 1, app, q, spin_bytes=sb, seed=seed)
+    lat.set_temperature(T)
+    lat.upload(spin)
+    done = 0
+    for calls in (1, 5, 4):
+        before = lat.launch_count()
+        lat.sweep(calls)
+        assert lat.launch_count() - before == 1  # one launch per call
+        done += calls
+        assert oracle.spin_hash(lat.download()) == int(hashes[done - 1]), (calls, done)
+    st = lat.stats()
+    assert (st["naccept"], st["nattempt"]) == (na, nt)
+    lat.close()
 
 
 def ensemble_case(seed=777):

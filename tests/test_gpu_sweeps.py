@@ -222,7 +222,7 @@ def test_fused_warp_sweeps_in_one_call_match_oracle(sg, T):
     cfg = oracle.make_cfg("sq/4n", nx, ny, 1, "ising", 2, T, seed=seed)
     ref = spin.copy()
     na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 10)
-    lat = sg.Lattice("sq/4n", nx, ny, 1, "ising", 2, spin_bytes=1, seed=seed)
+    lat = sg.Lattice("sq/4n", nx, ny, 1, "ising", 2, spin_bytes=1, seed=seed, variant=2)
     lat.set_temperature(T)
     lat.upload(spin)
     lat.sweep(7)
