@@ -3,7 +3,8 @@ statistical parity test of the Philox GPU path (tests/test_gpu_statistics.py).
 
 Runs ``oracle/_ref/spk_serial`` (the reference built from its own sources by
 ``oracle/ref/Makefile``, its own RandomPark / RanMars streams) with `sweep
-color` for NSEEDS seeds per configuration and records, from the last stats
+color`, or `solve_style tree` with `sector yes` for the KMC configuration, for
+NSEEDS seeds per configuration and records, from the last stats
 row of each run, the energy (diag_style energy), the mean site value
 (diag_style array i1 mean; Ising magnetisation 2*mean - 3) and the mean
 cluster volume <N> (diag_style cluster).  Writes reference_stats.json.
@@ -28,6 +29,12 @@ CONFIGS = [
     dict(name="ising_sq4n_64_T2.0", app="ising", q=2, lattice="sq/4n", n=(64, 64, 1), T=2.0, run=50.0),
     dict(name="potts_sq8n_48_Q10_T0.4", app="potts", q=10, lattice="sq/8n", n=(48, 48, 1), T=0.4, run=20.0),
     dict(name="ising_sc6n_16_T4.0", app="ising", q=2, lattice="sc/6n", n=(16, 16, 16), T=4.0, run=20.0),
+    # potts/neighonly on sc/26n (the C1 path): dt_sweep = 1/26, so run 19.5/26 is 19 sweeps
+    dict(name="neighonly_sc26n_12_Q20_T0.5", app="potts/neighonly", q=20, lattice="sc/26n", n=(12, 12, 12),
+         T=0.5, run=19.5 / 26),
+    # rejection-free KMC with the tree solver over four sectors (the C3 path), run to t = 2
+    dict(name="kmc_potts_sq8n_32_Q10_T0.8", app="potts", q=10, lattice="sq/8n", n=(32, 32, 1), T=0.8, run=2.0,
+         kmc=True),
 ]
 
 
@@ -38,7 +45,8 @@ def script(cfg, seed):
     app = "ising" if cfg["app"] == "ising" else f"{cfg['app']} {cfg['q']}"
     return [f"seed {seed}", f"app_style {app}", f"dimension {dim}", f"lattice {cfg['lattice']} 1.0",
             f"region box block 0 {nx} 0 {ny} {zrange}", "create_box box", "create_sites box",
-            f"set site range 1 {cfg['q']}", "sweep color", f"temperature {cfg['T']}", "diag_style energy",
+            f"set site range 1 {cfg['q']}"] + (["solve_style tree", "sector yes"] if cfg.get("kmc") else
+                                                  ["sweep color"]) + [f"temperature {cfg['T']}", "diag_style energy",
             "diag_style array i1 mean", "diag_style cluster", f"stats {cfg['run']}", f"run {cfg['run']}"]
 
 
@@ -68,14 +76,18 @@ def main():
     for cfg in CONFIGS:
         rows = [last_row(binary, script(cfg, 1000 + 7 * k)) for k in range(NSEEDS)]
         sweeps = {int(r["Nsweeps"]) for r in rows}
-        assert len(sweeps) == 1, sweeps
+        # a colour sweep run has the same sweep count for every seed; a KMC
+        # run ends at the same time, after a seed-dependent number of passes
+        assert cfg.get("kmc") or len(sweeps) == 1, sweeps
+        assert all(abs(float(r["Time"]) - cfg["run"]) < 1e-9 for r in rows) or not cfg.get("kmc")
         out["configs"].append({
-            **cfg, "script": script(cfg, "SEED"), "nsweeps": sweeps.pop(),
+            **cfg, "script": script(cfg, "SEED"), "nsweeps": None if cfg.get("kmc") else sweeps.pop(),
             "energy": [float(r["Energy"]) for r in rows],
             "mean_i1": [float(r["mean(i1)"]) for r in rows],
             "mean_volume": [float(r["<N>"]) for r in rows],
         })
-        print(cfg["name"], "sweeps", out["configs"][-1]["nsweeps"])
+        print(cfg["name"], "sweeps", out["configs"][-1]["nsweeps"], "mean energy",
+              sum(out["configs"][-1]["energy"]) / NSEEDS)
     (HERE / "reference_stats.json").write_text(json.dumps(out, indent=1))
     print("wrote", HERE / "reference_stats.json")
 

@@ -1,7 +1,8 @@
 """Statistical parity of the Philox GPU path with the unmodified reference:
 over independent seeds, the final energy, magnetisation (mean site value, and
 |m| = |2*mean - 3| for Ising) and mean cluster volume <N> of `sweep color`
-runs agree with the reference's own runs (its RandomPark/RanMars streams;
+runs (ising, potts, potts/neighonly) and of tree-KMC runs over sectors agree
+with the reference's own runs (its RandomPark/RanMars streams;
 tests/golden/reference_stats.json, made by make_reference_stats.py) within
 three standard errors of the difference of the two sample means."""
 
@@ -31,15 +32,29 @@ def within_3_sigma(a, b):
     return abs(a.mean() - b.mean()) <= 3.0 * se, a.mean(), b.mean(), se
 
 
-@pytest.mark.parametrize("cfg", REF["configs"], ids=lambda c: c["name"])
-def test_statistics_match_unmodified_reference(sg, cfg):
+CASES = [(c, None) for c in REF["configs"] if not c.get("kmc")] + \
+        [(c, fp64) for c in REF["configs"] if c.get("kmc") for fp64 in (True, False)]
+
+
+@pytest.mark.parametrize("cfg,fp64", CASES,
+                         ids=lambda v: v["name"] if isinstance(v, dict) else ("" if v is None else f"fp64={v}"))
+def test_statistics_match_unmodified_reference(sg, cfg, fp64):
+    """colour sweeps for the sweep configurations; for the tree-KMC one, runs
+    to the same time with FP64 propensities and with FP32 propensities (FP64
+    tree sums and clock)"""
     nx, ny, nz = cfg["n"]
     got = {"energy": [], "mean_i1": [], "mean_volume": []}
     for k in range(REF["nseeds"]):
-        lat = sg.Lattice(cfg["lattice"], nx, ny, nz, cfg["app"], cfg["q"], spin_bytes=1, seed=5000 + 11 * k)
+        kmc = cfg.get("kmc", False)
+        lat = sg.Lattice(cfg["lattice"], nx, ny, nz, cfg["app"], cfg["q"], spin_bytes=1, seed=5000 + 11 * k,
+                         nsector=4 if kmc else 1)
         lat.set_temperature(cfg["T"])
         lat.init_spins(1, cfg["q"])
-        lat.sweep(cfg["nsweeps"])
+        if kmc:
+            lat.kmc_setup(fp64=fp64)
+            assert lat.kmc_run(0.0, cfg["run"])["time"] == pytest.approx(cfg["run"], rel=1e-12)
+        else:
+            lat.sweep(cfg["nsweeps"])
         got["energy"].append(lat.energy())
         got["mean_i1"].append(lat.site_stats()["mean"])
         got["mean_volume"].append(lat.clusters()["mean_volume"])
