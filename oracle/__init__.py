@@ -61,6 +61,20 @@ def build_reference(jobs: int = 0) -> bool:
     return True
 
 
+def build_reference_gpu(jobs: int = 0) -> bool:
+    """Build oracle/_ref/spk_serial_gpu: the reference with the GPU app
+    styles of spparks_gb300/reference_app linked to libspkgpu.so (the
+    library must be built).  Returns False where no reference sources are."""
+    jobs = jobs or max(2, os.cpu_count() or 2)
+    ref = os.environ.get("SPK_REFERENCE_SRC", "/root/reference/src")
+    if not Path(ref, "app_lattice.cpp").exists():
+        if not Path(REF_STAGE, "app_lattice.cpp").exists():
+            return False
+        ref = str(REF_STAGE)
+    subprocess.check_call(["make", "-s", "-C", str(HERE / "ref"), f"-j{jobs}", f"REF={ref}", "gpu"])
+    return True
+
+
 def reference_binary(name: str = "runner_plain"):
     """Path of a reference binary built by build_reference, or None."""
     p = REF_OUT / name
