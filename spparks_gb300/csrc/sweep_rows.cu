@@ -49,9 +49,36 @@ __device__ __forceinline__ uint32_t first_appearance_small(int own, const int (&
   return first;
 }
 
-template <int NN, int APP, bool SMALLQ>
-__device__ __forceinline__ int update_rows(int own, const int (&nb)[NN], uint32_t x0, uint32_t x1, int nspins,
-                                           const uint64_t *thr) {
+// the value of neighbour j of the site at column x of the centre row, read
+// again from the staged rows (a runtime j: one shared-memory load instead of
+// a select over every neighbour)
+// (sq/8n and sc/26n: every offset in {-1,0,1}^d but 0, dx outer and dz
+// inner, so offset j is cell m = j or j+1 of that cube)
+template <typename S, int LAT>
+__device__ __forceinline__ int staged_neighbor(const S *rows, int nx, int x, int j) {
+  static_assert(LAT == SPKGPU_SQ_8N || LAT == SPKGPU_SC_26N, "row kernel lattices");
+  constexpr int MID = Stencil<LAT>::k3d ? 13 : 4;
+  const int m = j < MID ? j : j + 1;
+  int dx, dy, dz;
+  if (Stencil<LAT>::k3d) {
+    dx = m / 9 - 1;
+    dy = (m / 3) % 3 - 1;
+    dz = m % 3 - 1;
+  } else {
+    dx = m / 3 - 1;
+    dy = m % 3 - 1;
+    dz = 0;
+  }
+  int xn = x + dx;
+  xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
+  const int r = Stencil<LAT>::k3d ? (dz + 1) * 3 + (dy + 1) : dy + 1;
+  return (int)rows[r * nx + xn];
+}
+
+template <typename S, int LAT, int APP, bool SMALLQ>
+__device__ __forceinline__ int update_rows(int own, const int (&nb)[Stencil<LAT>::NN], uint32_t x0, uint32_t x1,
+                                           int nspins, const uint64_t *thr, const S *rows, int nx, int x) {
+  constexpr int NN = Stencil<LAT>::NN;
   if (APP == SPKGPU_ISING || APP == SPKGPU_POTTS) {
     int e0;
     return update_philox<NN, APP>(own, nb, x0, x1, nspins, thr, &e0);
@@ -70,7 +97,7 @@ __device__ __forceinline__ int update_rows(int own, const int (&nb)[NN], uint32_
     iran = scaled_pick((uint32_t)NN, x0);
     if ((int)iran >= nevent) return own;
   }
-  int news = pick_value<NN>(nb, __fns(first, 0, (int)iran + 1));
+  int news = staged_neighbor<S, LAT>(rows, nx, x, __fns(first, 0, (int)iran + 1));
   int e1 = count_unlike<NN>(news, nb);
   if (e1 <= e0) return news;
   return ((uint64_t)x1 < thr[e1 - e0]) ? news : own;  // thr is all 0 at zero temperature
@@ -145,7 +172,7 @@ __global__ void __launch_bounds__(512) row_pair_kernel(RowArgs a) {
         nb[j] = rows[r * nx + xn];
       }
       int own = rows[center * nx + x];
-      int news = update_rows<NN, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr);
+      int news = update_rows<S, LAT, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr, rows, nx, x);
       if (news != own) {
         rows[center * nx + x] = (S)news;
         spin[rowbase + x] = (S)news;
