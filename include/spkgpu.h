@@ -226,7 +226,7 @@ int spkgpu_sweep_sq4_noalloc(void *spin, int32_t nx, int32_t ny, int32_t spin_by
    barrier), or one launch per sweep over every tile of every replica with
    the exchange as separate launches; create times one captured step of each
    on the replica set and keeps the fastest (SPKGPU_ENSEMBLE_MODE=persistent,
-   launches, launches2, launches4 or warps in the environment forces one).  Each replica
+   launches, launches2, launches4, warps, warps2 or warps4 in the environment forces one).  Each replica
    follows the same per-site rule as a single `sweep color` lattice (same as
    spkgpu_sweep with sq/4n); replica r draws from Philox stream (r+1) << 8.
    The reference has no ensemble; it corresponds to running one reference
@@ -280,14 +280,17 @@ int spkgpu_ensemble_launch_count(const spkgpu_ensemble *e, int64_t *count);
 /* execution form in use and the autotuner's time of one step in each form
    (tune_ms[SPKGPU_ENSEMBLE_NMODES], ms; -1 where not timed); tune_ms may be
    NULL.  The per-sweep forms sweep 1, 2 or 4 consecutive tiles per CTA of
-   64 threads, or (warps, Ising only) one tile per warp, two tiles of one
-   replica per CTA. */
+   64 threads, or (warps, warps2, warps4; Ising only) one warp per tile, the
+   two warps of a CTA on two tiles of one replica, each warp sweeping 1, 2 or
+   4 tiles per launch one after another. */
 #define SPKGPU_ENSEMBLE_PERSISTENT 0
 #define SPKGPU_ENSEMBLE_LAUNCHES 1
 #define SPKGPU_ENSEMBLE_LAUNCHES2 2
 #define SPKGPU_ENSEMBLE_LAUNCHES4 3
 #define SPKGPU_ENSEMBLE_WARPS 4
-#define SPKGPU_ENSEMBLE_NMODES 5
+#define SPKGPU_ENSEMBLE_WARPS2 5
+#define SPKGPU_ENSEMBLE_WARPS4 6
+#define SPKGPU_ENSEMBLE_NMODES 7
 int spkgpu_ensemble_mode(const spkgpu_ensemble *e, int32_t *mode, float *tune_ms);
 /* device time (ms) of the sweep kernels in the most recent replay of the
    captured step and how many launches that covers (1 persistent kernel, or

@@ -74,7 +74,7 @@ class KmcStats(ctypes.Structure):
 
 # execution forms of an ensemble, in the order of SPKGPU_ENSEMBLE_* (spkgpu.h);
 # "warps" (one tile per warp) exists for Ising only
-ENSEMBLE_MODES = ("persistent", "launches", "launches2", "launches4", "warps")
+ENSEMBLE_MODES = ("persistent", "launches", "launches2", "launches4", "warps", "warps2", "warps4")
 
 
 class EnsembleDesc(ctypes.Structure):

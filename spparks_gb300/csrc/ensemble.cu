@@ -431,6 +431,41 @@ __global__ void __launch_bounds__(kTileThreads, APP == SPKGPU_ISING ? 32 : 12) e
 // last sweep before an exchange round): the tiles also add the replica's
 // unlike bonds after the sweep to a.bonds (warp_tile_bonds), in place of
 // ensemble_bonds_kernel.
+// this warp's tile of pair pb (none if the pair has one tile)
+template <bool AFTER_GRID, bool BONDS>
+__device__ __forceinline__ unsigned int warp_pair_tile(const EnsArgs &a, int pb, int warp, int lane, int parity,
+                                                       uint32_t sweep, int8_t *stage) {
+  const int t = a.pair_tile[2 * pb + warp];
+  if (t < 0) return 0;
+  const int r = a.pair_rep[pb];
+  const int L = a.L[r];
+  const int64_t base = a.base[r];
+  const int pos = a.tile_pos[t].y;
+  TileJob j;
+  j.src = (const int8_t *)(parity ? a.buf1 : a.buf0) + base;
+  j.dst = (int8_t *)(parity ? a.buf0 : a.buf1) + base;
+  j.L = L;
+  j.Ly = L;
+  j.x0 = (pos & 0xFFFF) * kTile;
+  j.y0 = (pos >> 16) * kTile;
+  j.base = 0;
+  j.seed = a.seed;
+  j.key1 = ((uint32_t)(r + 1) << 8) | kStreamSweep;
+  j.sweep = sweep;
+  j.nspins = a.nspins;
+  j.replica = a.tidx[r];
+  j.thr = a.thr + (int64_t)j.replica * 5;
+  j.t2 = j.thr[2];
+  j.t4 = j.thr[4];
+  unsigned int bonds = 0;
+  const unsigned int changed = warp_tile_ising8<AFTER_GRID, BONDS>(j, stage, lane, &bonds);
+  if (BONDS) {
+    const unsigned int b = __reduce_add_sync(0xFFFFFFFFu, bonds);
+    if (lane == 0 && b) atomicAdd(&a.bonds[r], (unsigned long long)b);
+  }
+  return changed;
+}
+
 template <bool AFTER_GRID, bool BONDS>
 __global__ void __launch_bounds__(64, 20) ensemble_warp_kernel(EnsArgs a, int k) {
   __shared__ __align__(16) int8_t stage[2][kWStageBytes];
@@ -468,6 +503,31 @@ __global__ void __launch_bounds__(64, 20) ensemble_warp_kernel(EnsArgs a, int k)
     const unsigned int b = __reduce_add_sync(0xFFFFFFFFu, bonds);
     if (lane == 0 && b) atomicAdd(&a.bonds[r], (unsigned long long)b);
   }
+}
+
+// warps2 / warps4: CTA b sweeps pairs b*TPW .. b*TPW+TPW-1, each warp its
+// tile of each pair in turn; only the first tile waits for the previous
+// grid, and the warp's lanes finish reading the stage before the next tile
+// is staged.  Warps that run several tiles drift apart in phase, so the
+// ALU-heavy colour phases of some overlap the multiply-heavy draws of others.
+template <bool AFTER_GRID, bool BONDS, int TPW>
+__global__ void __launch_bounds__(64, 16) ensemble_warp_multi_kernel(EnsArgs a, int k) {
+  __shared__ __align__(16) int8_t stage[2][kWStageBytes];
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int parity = *(volatile int *)&a.ctl->parity ^ (k & 1);
+  const uint32_t sweep = *(volatile uint32_t *)&a.ctl->sweep + (uint32_t)k;
+  const int pb0 = blockIdx.x * TPW;
+  unsigned int changed = warp_pair_tile<AFTER_GRID, BONDS>(a, pb0, warp, lane, parity, sweep, stage[warp]);
+#pragma unroll 1
+  for (int q = 1; q < TPW; q++) {
+    if (pb0 + q >= a.npairs) break;
+    __syncwarp();
+    changed += warp_pair_tile<false, BONDS>(a, pb0 + q, warp, lane, parity, sweep, stage[warp]);
+  }
+  const unsigned int w = __reduce_add_sync(0xFFFFFFFFu, changed);
+  if (lane == 0 && w)
+    atomicAdd(&a.nacc_slots[(2 * blockIdx.x + warp) & (kCounterSlots - 1)], (unsigned long long)w);
 }
 
 // unlike bonds (right and down neighbour of each site) of every replica in
@@ -611,27 +671,54 @@ static cudaError_t ens_launch(spkgpu_ensemble *e, int nsweeps) {
   return cudaLaunchCooperativeKernel(e->kfn, dim3(e->grid), dim3(kTileThreads), params, 0, e->stream);
 }
 
+// the warp forms: one, two or four tiles per warp and launch
+static bool is_warp_mode(int mode) {
+  return mode == SPKGPU_ENSEMBLE_WARPS || mode == SPKGPU_ENSEMBLE_WARPS2 || mode == SPKGPU_ENSEMBLE_WARPS4;
+}
+
+// the warp form with TPW tile pairs per CTA; after_grid: launched as a
+// programmatic dependent of the previous sweep
+template <bool AG, bool BONDS, int TPW>
+static constexpr auto warp_kernel() {
+  if constexpr (TPW == 1) return ensemble_warp_kernel<AG, BONDS>;
+  else return ensemble_warp_multi_kernel<AG, BONDS, TPW>;
+}
+
+template <int TPW>
+static void launch_warp_t(bool after_grid, bool bonds, unsigned g, const EnsArgs &a, int k, cudaStream_t st) {
+  if (!after_grid) {
+    if (bonds) warp_kernel<false, true, TPW>()<<<g, 64, 0, st>>>(a, k);
+    else warp_kernel<false, false, TPW>()<<<g, 64, 0, st>>>(a, k);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g);
+  cfg.blockDim = dim3(64);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (bonds) cudaLaunchKernelEx(&cfg, warp_kernel<true, true, TPW>(), a, k);
+  else cudaLaunchKernelEx(&cfg, warp_kernel<true, false, TPW>(), a, k);
+}
+
+static void launch_warp_sweep(int tpw, bool after_grid, bool bonds, unsigned g, const EnsArgs &a, int k,
+                              cudaStream_t st) {
+  if (tpw == 4) launch_warp_t<4>(after_grid, bonds, g, a, k, st);
+  else if (tpw == 2) launch_warp_t<2>(after_grid, bonds, g, a, k, st);
+  else launch_warp_t<1>(after_grid, bonds, g, a, k, st);
+}
+
 // one sweep launch of the per-sweep forms (1, 2 or 4 tiles per CTA)
 // (warp form: `bonds` = the last sweep before an exchange round counts the
 // replicas' unlike bonds itself)
 static void launch_sweep(const spkgpu_ensemble *e, const EnsArgs &a, int k, cudaStream_t st, bool bonds) {
-  if (e->mode == SPKGPU_ENSEMBLE_WARPS) {
-    if (k == 0) {
-      if (bonds) ensemble_warp_kernel<false, true><<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
-      else ensemble_warp_kernel<false, false><<<(unsigned)a.npairs, 64, 0, st>>>(a, k);
-      return;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)a.npairs);
-    cfg.blockDim = dim3(64);
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (bonds) cudaLaunchKernelEx(&cfg, ensemble_warp_kernel<true, true>, a, k);
-    else cudaLaunchKernelEx(&cfg, ensemble_warp_kernel<true, false>, a, k);
+  if (is_warp_mode(e->mode)) {
+    const int tpw = e->mode == SPKGPU_ENSEMBLE_WARPS4 ? 4 : (e->mode == SPKGPU_ENSEMBLE_WARPS2 ? 2 : 1);
+    const unsigned g = (unsigned)((a.npairs + tpw - 1) / tpw);
+    launch_warp_sweep(tpw, k > 0, bonds, g, a, k, st);
     return;
   }
   const int tpc = e->mode == SPKGPU_ENSEMBLE_LAUNCHES4 ? 4 : (e->mode == SPKGPU_ENSEMBLE_LAUNCHES2 ? 2 : 1);
@@ -653,7 +740,7 @@ static cudaError_t ens_launch_group(spkgpu_ensemble *e, int m, bool exchange, in
   const EnsArgs &a = e->args;
   const unsigned nt = (unsigned)e->ntiles;
   // the warp form counts the bonds in the last sweep of the group
-  const bool sweep_bonds = exchange && e->mode == SPKGPU_ENSEMBLE_WARPS;
+  const bool sweep_bonds = exchange && is_warp_mode(e->mode);
   for (int k = 0; k < m; k++) launch_sweep(e, a, k, e->stream, sweep_bonds && k == m - 1);
   if (exchange && !sweep_bonds)
     ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, e->stream>>>(a, m);
@@ -666,7 +753,7 @@ static cudaError_t ens_launch_group(spkgpu_ensemble *e, int m, bool exchange, in
 static int64_t ens_step_kernels(const spkgpu_ensemble *e) {
   if (e->mode == SPKGPU_ENSEMBLE_PERSISTENT) return 1;
   const bool exchange = e->d.exchange_every > 0;
-  return e->chunk + (exchange && e->mode != SPKGPU_ENSEMBLE_WARPS ? 1 : 0) + 1;
+  return e->chunk + (exchange && !is_warp_mode(e->mode) ? 1 : 0) + 1;
 }
 
 // captures one step (chunk sweeps, ending on an exchange point when
@@ -693,7 +780,7 @@ static void ens_capture(spkgpu_ensemble *e) {
     const EnsArgs &a = e->args;
     const unsigned nt = (unsigned)e->ntiles;
     const bool exchange = e->d.exchange_every > 0;
-    const bool sweep_bonds = exchange && e->mode == SPKGPU_ENSEMBLE_WARPS;
+    const bool sweep_bonds = exchange && is_warp_mode(e->mode);
     for (int k = 0; k < e->chunk; k++) launch_sweep(e, a, k, cap, sweep_bonds && k == e->chunk - 1);
     kev = kev && cudaEventRecordWithFlags(e->kev1, cap, cudaEventRecordExternal) == cudaSuccess;
     if (exchange && !sweep_bonds)
@@ -744,11 +831,11 @@ static cudaError_t ens_reset(spkgpu_ensemble *e) {
 // SPKGPU_ENSEMBLE_MODE=persistent|launches|launches2|launches4|warps forces a
 // mode (warps only for Ising).
 static const char *const kModeNames[SPKGPU_ENSEMBLE_NMODES] = {"persistent", "launches", "launches2", "launches4",
-                                                                "warps"};
+                                                                "warps", "warps2", "warps4"};
 
 // the warp form sweeps Ising sites only
 static bool ens_mode_ok(const spkgpu_ensemble *e, int mode) {
-  return mode != SPKGPU_ENSEMBLE_WARPS || e->d.app == SPKGPU_ISING;
+  return !is_warp_mode(mode) || e->d.app == SPKGPU_ISING;
 }
 
 static int ens_pick_mode(spkgpu_ensemble *e, float *ms_out) {
