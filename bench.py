@@ -683,11 +683,12 @@ def measure_configs_c3(sg, serial_t=0.02):
     written) and on a 32x32 processor grid, events/s (host clock around a
     synchronous run, after a short warm-up pass)."""
     res = {}
-    for name, procs, tend in (("C3_serial", (1, 1, 1), serial_t), ("C3_grid", (32, 32, 1), 1.0)):
+    for name, procs, tend, fp64 in (("C3_serial", (1, 1, 1), serial_t, True), ("C3_grid", (32, 32, 1), 1.0, True),
+                                    ("C3_serial_fp32", (1, 1, 1), serial_t, False)):
         lat = sg.Lattice("sq/8n", 2048, 2048, 1, "potts", 50, spin_bytes=4, nsector=4, procs=procs, seed=SEED)
         lat.set_temperature(1.0)
         lat.init_spins(1, 50)
-        lat.kmc_setup(fp64=True)
+        lat.kmc_setup(fp64=fp64)
         w = lat.kmc_run(0.0, 1e-4)  # warm-up: one short pass (tree build, first kernels)
         t0 = time.perf_counter()
         st = lat.kmc_run(w["time"], w["time"] + tend)
@@ -695,10 +696,14 @@ def measure_configs_c3(sg, serial_t=0.02):
         ev = st["naccept"] - w["naccept"]
         lat.close()
         res[name] = {"workload": f"2048^2 sq/8n potts Q=50 kT 1, tree KMC, 4 sectors, processors "
-                                 f"{procs[0]}x{procs[1]}, FP64 propensities, t += {tend}",
+                                 f"{procs[0]}x{procs[1]}, {'FP64' if fp64 else 'FP32 (FP64 tree and clock)'} "
+                                 f"propensities, t += {tend}",
                      "value": ev / wall, "unit": "events/s", "events": ev, "passes": st["npass"],
                      "roofline": {"bound": "latency", "frac": None,
                                   "note": "a chain of dependent events per sector; the HBM fraction is not meaningful"}}
+        if not fp64:
+            res[name]["errors"] = {"prop_rel_err": st["prop_rel_err"], "dt_rel_err": st["dt_rel_err"],
+                                   "against": "all-FP64 propensities of the same chains"}
     return res
 
 
