@@ -651,24 +651,28 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
         bool found = false;
         if (a.fp64) {
           const double term = !live ? 0.0 : (e1 <= e0 ? 1.0 : (a.zero_t ? 0.0 : a.pexp[e1 - e0]));
+          double tj[NN];
+#pragma unroll
+          for (int j = 0; j < NN; j++) tj[j] = __shfl_sync(FULL, term, j);
           double prob = 0.0;
 #pragma unroll
           for (int j = 0; j < NN; j++) {
-            const double tj = __shfl_sync(FULL, term, j);
             if (!found && ((first >> j) & 1u)) {
-              prob += tj;
+              prob += tj[j];
               val = nb[j];
               found = nonneg_le(threshhold, prob);  // prob >= threshhold
             }
           }
         } else {
           const float term = !live ? 0.0f : (e1 <= e0 ? 1.0f : (a.zero_t ? 0.0f : a.pexpf[e1 - e0]));
+          float tj[NN];
+#pragma unroll
+          for (int j = 0; j < NN; j++) tj[j] = __shfl_sync(FULL, term, j);
           float prob = 0.0f;
 #pragma unroll
           for (int j = 0; j < NN; j++) {
-            const float tj = __shfl_sync(FULL, term, j);
             if (!found && ((first >> j) & 1u)) {
-              prob += tj;
+              prob += tj[j];
               val = nb[j];
               found = nonneg_le(threshhold, (double)prob);
             }
@@ -770,31 +774,29 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
       }
       __syncwarp();
     }
-    double root = 0.0;
-    if (lane == 0) {
-      double v = top[nd];
-      const int lev = 31 - __clz(nd + 1);  // levels above nd
-      double sv[kTopLevels];
-      int sn = nd;
-#pragma unroll
-      for (int q = 0; q < kTopLevels; q++) {
-        if (q < lev) {
-          sv[q] = top[(sn & 1) ? sn + 1 : sn - 1];
-          sn = (sn - 1) >> 1;
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < kTopLevels; q++) {
-        if (q < lev) {
-          const bool left = nd & 1;
-          nd = (nd - 1) >> 1;
-          v = left ? v + sv[q] : sv[q] + v;
-          top[nd] = v;
-        }
-      }
-      root = v;
+    // the single path above the common ancestor: lane q fetches the sibling
+    // q levels up, then every lane adds them in turn (the same sums on every
+    // lane, lane 0 stores them); lane 0 is always on the path
+    const int top_nd = __shfl_sync(FULL, nd, 0);
+    const int lev = 31 - __clz(top_nd + 1);  // levels above it, the same on every lane
+    double sib = 0.0;
+    if (lane < lev) {
+      const int anc = ((top_nd + 1) >> lane) - 1;
+      sib = top[(anc & 1) ? anc + 1 : anc - 1];
     }
-    sum = __shfl_sync(FULL, root, 0);
+    double v = top[top_nd];
+    int n = top_nd;
+#pragma unroll
+    for (int q = 0; q < kTopLevels; q++) {
+      if (q < lev) {
+        const double sq = __shfl_sync(FULL, sib, q);
+        const bool left = n & 1;
+        n = (n - 1) >> 1;
+        v = left ? v + sq : sq + v;
+        if (lane == 0) top[n] = v;
+      }
+    }
+    sum = v;
     __syncwarp();
     done_events++;
   }
