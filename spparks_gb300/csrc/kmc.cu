@@ -520,40 +520,83 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
     // src/solve_tree.cpp:130-143)
     const double dt = -1.0 / sum * lu;
     // SolveTree::find through the cached levels (src/solve_tree.cpp:207-224)
+    // every lane walks (the same loads and decisions on every lane: no
+    // divergence, no broadcast afterwards)
+    // Two levels per step: the left child and both grandchildren that can
+    // come next are read together, then the two decisions are taken in turn.
     int node = 0;
     double value = ux * sum;
-    if (lane == 0) {
-      const int stop = whole ? leaf0 : (kTopNodes >> 1);  // children of nodes below it are cached
-      while (node < stop) {
-        const int left = 2 * node + 1;
-        const double tl = top[left];
-        if (nonneg_le(value, tl)) node = left;
+    {
+      int steps = whole ? depth : kTopLevels - 1;  // down to the leaves or to level 13
+      for (; steps >= 2; steps -= 2) {
+        const int l = 2 * node + 1;
+        const double tl = top[l], tll = top[2 * l + 1], trl = top[2 * l + 3];
+        if (nonneg_le(value, tl)) {
+          node = l;
+          if (nonneg_le(value, tll)) node = 2 * l + 1;
+          else {
+            value -= tll;
+            node = 2 * l + 2;
+          }
+        } else {
+          value -= tl;
+          node = l + 1;
+          if (nonneg_le(value, trl)) node = 2 * l + 3;
+          else {
+            value -= trl;
+            node = 2 * l + 4;
+          }
+        }
+      }
+      if (steps) {
+        const int l = 2 * node + 1;
+        const double tl = top[l];
+        if (nonneg_le(value, tl)) node = l;
         else {
           value -= tl;
-          node = left + 1;
+          node = l + 1;
         }
       }
     }
-    node = __shfl_sync(FULL, node, 0);
     double *SF = slots + (size_t)(NSLOT - 1) * slotn;  // the pick's slot
     if (!whole) {
       // node is the level-13 node A: its descendants in one round trip
       load_slot(G, SF, node, slotn, lane);
       cp_async_wait_all();
       __syncwarp();
-      if (lane == 0) {
-        const int A = node;
-        for (int j = 0; j < hb; j++) {
-          const int left = 2 * node + 1;
-          const double tl = SF[left - (A << (j + 1)) - 1];
-          if (nonneg_le(value, tl)) node = left;
+      const int A = node;
+      int j = 0;  // depth of node below A
+      for (; j + 2 <= hb; j += 2) {
+        const int l = 2 * node + 1;
+        const int tl_at = l - (A << (j + 1)) - 1;
+        const int g0 = 2 * l + 1 - (A << (j + 2)) - 1;  // left child of l; +2: left child of l + 1
+        const double tl = SF[tl_at], tll = SF[g0], trl = SF[g0 + 2];
+        if (nonneg_le(value, tl)) {
+          node = l;
+          if (nonneg_le(value, tll)) node = 2 * l + 1;
           else {
-            value -= tl;
-            node = left + 1;
+            value -= tll;
+            node = 2 * l + 2;
+          }
+        } else {
+          value -= tl;
+          node = l + 1;
+          if (nonneg_le(value, trl)) node = 2 * l + 3;
+          else {
+            value -= trl;
+            node = 2 * l + 4;
           }
         }
       }
-      node = __shfl_sync(FULL, node, 0);
+      if (j < hb) {
+        const int l = 2 * node + 1;
+        const double tl = SF[l - (A << (j + 1)) - 1];
+        if (nonneg_le(value, tl)) node = l;
+        else {
+          value -= tl;
+          node = l + 1;
+        }
+      }
     }
     const int m = node - leaf0;
     timesector += dt;
