@@ -17,6 +17,8 @@
 #include <algorithm>
 #include <new>
 #include <string>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "counters.cuh"
@@ -126,6 +128,70 @@ int sector_half(int nsector, int sector, int axis) {
 }
 
 }  // namespace
+
+// Where an sq/4n lattice fits one cluster, both the cluster-resident sweep
+// (every sweep of a call in one launch) and the tile kernel (one launch per
+// sweep) apply; they give the same lattice.  The first handle of each
+// (device, app, width, nx, ny) times four sweeps of each on a scratch copy
+// (Philox initial values, temperature 1) and keeps the faster for every
+// later handle of that shape in the process.
+static bool resident_is_faster(spkgpu_lattice *h) {
+  static std::mutex mu;
+  static std::map<std::vector<int>, bool> cache;
+  const spkgpu_desc &d = h->d;
+  const std::vector<int> key{d.device, d.app, h->spin_bytes, d.nx, d.ny};
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  const size_t bytes = (size_t)h->n * h->spin_bytes;
+  void *a = nullptr, *b = nullptr;
+  unsigned long long *cnt = nullptr;
+  bool resident = false;  // the tile kernel, should a timing step fail
+  if (cudaMalloc(&a, bytes) == cudaSuccess && cudaMalloc(&b, bytes) == cudaSuccess &&
+      cudaMalloc(&cnt, spk::kCounterSlots * sizeof(unsigned long long)) == cudaSuccess) {
+    spk::AcceptTable acc;
+    spk::build_accept_table(1.0, d.app, &acc);
+    cudaStream_t st = h->stream;
+    const int nsw = 4;
+    float ms[2] = {0.0f, 0.0f};
+    bool ok = spk::launch_init(h->spin_bytes, a, h->n, d.seed, 1, d.nspins, st, h->num_sms) == cudaSuccess;
+    for (int form = 0; form < 2 && ok; form++) {
+      for (int rep = 0; rep < 2 && ok; rep++) {  // the first pass warms up
+        ok = cudaEventRecord(h->ev0, st) == cudaSuccess;
+        if (form == 0) {
+          ok = ok && spk::launch_resident_sweeps(d.app, h->spin_bytes, a, d.nx, d.ny, d.seed, 0, nsw, d.nspins, cnt,
+                                                 acc, st) == cudaSuccess;
+        } else {
+          for (int k = 0; k < nsw && ok; k++) {
+            spk::FusedArgs f;
+            f.src = (k & 1) ? b : a;
+            f.dst = (k & 1) ? a : b;
+            f.nx = d.nx;
+            f.ny = d.ny;
+            f.seed = d.seed;
+            f.sweep = (uint32_t)k;
+            f.nspins = d.nspins;
+            f.naccept = cnt;
+            f.acc = acc;
+            ok = spk::launch_fused2d(d.lattice, d.app, h->spin_bytes, f, st, h->num_sms) == cudaSuccess;
+          }
+        }
+        ok = ok && cudaEventRecord(h->ev1, st) == cudaSuccess && cudaEventSynchronize(h->ev1) == cudaSuccess &&
+             cudaEventElapsedTime(&ms[form], h->ev0, h->ev1) == cudaSuccess;
+      }
+    }
+    if (ok) resident = ms[0] <= ms[1];
+    cudaGetLastError();
+  }
+  cudaFree(a);
+  cudaFree(b);
+  cudaFree(cnt);
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = resident;
+  return resident;
+}
 
 extern "C" {
 
@@ -242,7 +308,8 @@ int spkgpu_create(const spkgpu_desc *desc, spkgpu_lattice **out) {
   h->fused_ok = (!packed && (d.variant == 0 || d.variant == 2) && d.nsector == 1 && d.nloop == 1 &&
                  d.rng == SPKGPU_RNG_PHILOX && !d.mask &&
                  spk::fused2d_supported(d.lattice, d.app, sb, d.nx, d.ny));
-  h->resident_ok = h->fused_ok && d.variant == 0 && spk::resident_supported(d.lattice, d.app, sb, d.nx, d.ny);
+  h->resident_ok = h->fused_ok && d.variant == 0 && spk::resident_supported(d.lattice, d.app, sb, d.nx, d.ny) &&
+                   resident_is_faster(h);
   if (h->fused_ok) {
     if (cudaMalloc(&h->d_spin_alt, (size_t)h->n * sb) != cudaSuccess) return fail(SPKGPU_ERR_NOMEM);
   }
