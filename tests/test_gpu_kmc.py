@@ -138,3 +138,37 @@ def test_kmc_run_in_pieces_equals_one_run(sg):
         finals.append((st["naccept"], st["npass"], st["time"], lat.download().tolist()))
         lat.close()
     assert finals[0] == finals[1]
+
+
+SERIAL_TREE_CASES = [
+    # one processor: chains large enough that only the top 14 tree levels stay in shared memory and the
+    # rest is fetched per event (3d site blocks of 125 values, box sides that are not powers of two)
+    dict(lattice="sc/26n", nx=96, ny=96, nz=96, app="potts", nspins=20, T=0.8, nsector=8, run=0.004),
+    dict(lattice="sc/6n", nx=64, ny=64, nz=64, app="ising", nspins=2, T=3.0, nsector=2, run=0.02),
+    dict(lattice="sq/4n", nx=768, ny=512, nz=1, app="potts/neighonly", nspins=12, T=0.6, nsector=4, run=0.01),
+]
+
+
+@pytest.mark.parametrize("c", SERIAL_TREE_CASES, ids=lambda c: f"{c['app']}-{c['lattice']}-{c['nx']}")
+def test_kmc_large_chains_match_oracle(sg, c):
+    """serial chains whose trees exceed the shared-memory levels: the event
+    loop fetches subtrees and paths from the global tree; lattice, events,
+    passes and clock equal the oracle's"""
+    seed = 97
+    n = c["nx"] * c["ny"] * c["nz"]
+    spin = oracle.init_spins(seed, n, 1, c["nspins"])
+    cfg = oracle.make_cfg(c["lattice"], c["nx"], c["ny"], c["nz"], c["app"], c["nspins"], c["T"], c["nsector"],
+                          seed=seed)
+    km = oracle.Kmc(cfg)
+    ref = spin.copy()
+    npass, _, _ = km.run(ref, c["run"])
+    assert km.naccept > 1000
+    lat = sg.Lattice(c["lattice"], c["nx"], c["ny"], c["nz"], c["app"], c["nspins"], nsector=c["nsector"], seed=seed)
+    lat.set_temperature(c["T"])
+    lat.upload(spin)
+    lat.kmc_setup(fp64=True)
+    st = lat.kmc_run(0.0, c["run"])
+    assert oracle.spin_hash(lat.download()) == oracle.spin_hash(ref)
+    assert (st["naccept"], st["npass"]) == (km.naccept, npass)
+    assert st["time"] == pytest.approx(km.time, rel=1e-12)
+    lat.close()
