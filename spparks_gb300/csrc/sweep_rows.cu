@@ -12,8 +12,9 @@
 // order (src/app_lattice.cpp:672-680).
 //
 // The distinct-value list of potts/neighonly and potts/neigh
-// (src/app_potts_neighonly.cpp:80-88) is built with a 128-bit seen-set when
-// every value is below 128, else with the pairwise scan.
+// (src/app_potts_neighonly.cpp:80-88) is built with a 128-bit seen-set in the
+// thread's 16 bytes of shared memory when every value is below 128, else with
+// the pairwise scan.
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -23,31 +24,6 @@
 #include "spk_internal.h"
 
 namespace spk {
-
-// first-appearance mask of the distinct values != own among nb[] (values
-// 1..127): one test-and-set per neighbour in a 128-bit seen-set held as two
-// 64-bit words
-template <int NN>
-__device__ __forceinline__ uint32_t first_appearance_small(int own, const int (&nb)[NN]) {
-  uint64_t lo = 0, hi = 0;
-  {
-    uint64_t b = 1ull << (own & 63);
-    if (own & 64) hi = b;
-    else lo = b;
-  }
-  uint32_t first = 0;
-#pragma unroll
-  for (int j = 0; j < NN; j++) {
-    int v = nb[j];
-    uint64_t b = 1ull << (v & 63);
-    bool upper = (v & 64) != 0;
-    uint64_t cur = upper ? hi : lo;
-    first |= ((cur & b) ? 0u : 1u) << j;
-    hi |= upper ? b : 0ull;
-    lo |= upper ? 0ull : b;
-  }
-  return first;
-}
 
 // the value of neighbour j of the site at column x of the centre row, read
 // again from the staged rows (a runtime j: one shared-memory load instead of
@@ -75,9 +51,30 @@ __device__ __forceinline__ int staged_neighbor(const S *rows, int nx, int x, int
   return (int)rows[r * nx + xn];
 }
 
+// first-appearance mask of the distinct values != own among nb[] (values
+// 1..127; first_appearance's result) from a 128-bit seen-set in this
+// thread's four words of shared memory: a load, a test and a store per
+// neighbour
+template <int NN>
+__device__ __forceinline__ uint32_t first_appearance_shared(int own, const int (&nb)[NN], uint32_t *seen) {
+  *(uint4 *)seen = make_uint4(0u, 0u, 0u, 0u);
+  seen[own >> 5] = 1u << (own & 31);
+  uint32_t first = 0;
+#pragma unroll
+  for (int j = 0; j < NN; j++) {
+    const int v = nb[j];
+    const uint32_t b = 1u << (v & 31);
+    const uint32_t cur = seen[v >> 5];
+    first |= ((cur & b) ? 0u : 1u) << j;
+    seen[v >> 5] = cur | b;
+  }
+  return first;
+}
+
 template <typename S, int LAT, int APP, bool SMALLQ>
 __device__ __forceinline__ int update_rows(int own, const int (&nb)[Stencil<LAT>::NN], uint32_t x0, uint32_t x1,
-                                           int nspins, const uint64_t *thr, const S *rows, int nx, int x) {
+                                           int nspins, const uint64_t *thr, const S *rows, int nx, int x,
+                                           uint32_t *seen) {
   constexpr int NN = Stencil<LAT>::NN;
   if (APP == SPKGPU_ISING || APP == SPKGPU_POTTS) {
     int e0;
@@ -86,7 +83,7 @@ __device__ __forceinline__ int update_rows(int own, const int (&nb)[Stencil<LAT>
   int e0 = count_unlike<NN>(own, nb);
   // no unlike neighbour: no event and no draw (nevent == 0 below)
   if (e0 == 0) return own;
-  uint32_t first = SMALLQ ? first_appearance_small<NN>(own, nb) : first_appearance<NN>(own, nb);
+  uint32_t first = SMALLQ ? first_appearance_shared<NN>(own, nb, seen) : first_appearance<NN>(own, nb);
   int nevent = __popc(first);
   uint32_t iran;
   if (APP == SPKGPU_POTTS_NEIGHONLY) {
@@ -120,6 +117,9 @@ __global__ void __launch_bounds__(512) row_pair_kernel(RowArgs a) {
   constexpr int NROWS = Stencil<LAT>::k3d ? 9 : 3;
   extern __shared__ __align__(16) unsigned char row_smem[];
   S *rows = (S *)row_smem;
+  // 16 bytes of seen-set per thread after the rows (16-byte aligned)
+  const size_t rows_bytes = ((size_t)NROWS * a.nx * sizeof(S) + 15) & ~(size_t)15;
+  uint32_t *seen = (uint32_t *)(row_smem + rows_bytes) + 4 * threadIdx.x;
   __shared__ uint64_t thr[kMaxNeigh + 1];
   if (threadIdx.x <= kMaxNeigh) thr[threadIdx.x] = a.acc.thr[threadIdx.x];
   const int nx = a.nx;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(512) row_pair_kernel(RowArgs a) {
         nb[j] = rows[r * nx + xn];
       }
       int own = rows[center * nx + x];
-      int news = update_rows<S, LAT, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr, rows, nx, x);
+      int news = update_rows<S, LAT, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr, rows, nx, x, seen);
       if (news != own) {
         rows[center * nx + x] = (S)news;
         spin[rowbase + x] = (S)news;
@@ -195,8 +195,8 @@ static cudaError_t launch_rows_app(const RowArgs &a, bool smallq, cudaStream_t s
   int rows_y = (a.ny - a.qy + 1) / 2;
   int rows_z = Stencil<LAT>::k3d ? (a.nz - a.qz + 1) / 2 : 1;
   unsigned grid = (unsigned)(rows_y * rows_z);
-  size_t smem = (size_t)NROWS * a.nx * sizeof(S);
   int threads = ((a.nx / 2 + 31) / 32) * 32;  // one x-pair per thread
+  size_t smem = (((size_t)NROWS * a.nx * sizeof(S) + 15) & ~(size_t)15) + (size_t)threads * 16;
   if (smallq) {
     auto f = row_pair_kernel<S, LAT, APP, true>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
