@@ -742,6 +742,7 @@ def kernel_case(name):
     elif name == "rates":  # site-updates/s of the single-lattice sweeps, CUDA events on each lattice's stream
         cases = [
             ("sq/4n 128^2 ising int32, 100 sweeps", ("sq/4n", 128, 128, 1, "ising", 2, 4), 2.269, 100),
+            ("sc/26n 256^3 potts/neighonly Q=100 int16", ("sc/26n", 256, 256, 256, "potts/neighonly", 100, 2), 0.5, 5),
             ("sc/6n 1536^3 ising bit-packed", ("sc/6n", 1536, 1536, 1536, "ising", 2, -1), 4.5115, 3),
             ("sc/6n 1536^3 ising int8", ("sc/6n", 1536, 1536, 1536, "ising", 2, 1), 4.5115, 2),
             ("sq/4n 12288^2 ising int8", ("sq/4n", 12288, 12288, 1, "ising", 2, 1), 2.269, 20),

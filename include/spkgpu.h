@@ -264,8 +264,8 @@ int spkgpu_ensemble_timed_run(spkgpu_ensemble *e, int32_t nsweeps, float *ms);
    result into `out` (host, int32), and return at once.  With page-locked
    buffers (cudaHostAlloc or cudaHostRegister) the copy engines move a call's
    input while the previous call's sweeps run and its result while the next
-   call's sweeps run (two int32 device staging buffers of every site are
-   allocated on the first call).  Both buffers must stay untouched until
+   call's sweeps run (four int32 device staging buffers of every site, two
+   per direction used by alternate calls, are allocated on the first call).  Both buffers must stay untouched until
    spkgpu_ensemble_synchronize returns; that call reports invalid input values
    (SPKGPU_ERR_INVALID_SPIN), found after the sweeps have run on them.
    Pageable buffers take upload, run and download in turn (synchronous). */

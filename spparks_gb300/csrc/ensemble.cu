@@ -618,11 +618,13 @@ struct spkgpu_ensemble {
   float tune_ms[SPKGPU_ENSEMBLE_NMODES] = {-1.0f, -1.0f, -1.0f, -1.0f, -1.0f};  // the autotuner's step times per mode
   int32_t *d_pair_rep = nullptr, *d_pair_tile = nullptr;
   int npairs = 0;
-  // pipelined host I/O (spkgpu_ensemble_run_io): int32 device staging of
-  // the input and the output, one copy stream per direction, events between
-  int32_t *io_in32 = nullptr, *io_out32 = nullptr;
+  // pipelined host I/O (spkgpu_ensemble_run_io): two int32 device staging
+  // buffers of the input and two of the output (call k uses pair k % 2), one
+  // copy stream per direction, events between
+  int32_t *io_in32[2] = {nullptr, nullptr}, *io_out32[2] = {nullptr, nullptr};
   cudaStream_t io_in = nullptr, io_out = nullptr;
-  cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_snap_ready = nullptr, ev_snap_free = nullptr;
+  cudaEvent_t ev_in_ready[2] = {}, ev_in_free[2] = {}, ev_snap_ready[2] = {}, ev_snap_free[2] = {};
+  int io_calls = 0;
   bool io_pending = false;  // run_io calls since the last synchronize (bad-value flag armed)
   int64_t enq = 0;  // sweeps enqueued so far (the host's copy of ctl->sweep)
   std::vector<int32_t> slot_init;  // replica in each exchange slot at creation
@@ -918,10 +920,12 @@ int spkgpu_ensemble_destroy(spkgpu_ensemble *e) {
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->kev0) cudaEventDestroy(e->kev0);
   if (e->kev1) cudaEventDestroy(e->kev1);
-  cudaFree(e->io_in32);
-  cudaFree(e->io_out32);
-  for (cudaEvent_t ev : {e->ev_in_ready, e->ev_in_free, e->ev_snap_ready, e->ev_snap_free})
-    if (ev) cudaEventDestroy(ev);
+  for (int b = 0; b < 2; b++) {
+    cudaFree(e->io_in32[b]);
+    cudaFree(e->io_out32[b]);
+    for (cudaEvent_t ev : {e->ev_in_ready[b], e->ev_in_free[b], e->ev_snap_ready[b], e->ev_snap_free[b]})
+      if (ev) cudaEventDestroy(ev);
+  }
   if (e->io_in) cudaStreamDestroy(e->io_in);
   if (e->io_out) cudaStreamDestroy(e->io_out);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -1219,26 +1223,34 @@ int spkgpu_ensemble_timed_run(spkgpu_ensemble *e, int32_t nsweeps, float *ms) {
   return SPKGPU_OK;
 }
 
-// Pipelined host I/O.  Per call, on three streams:
-//   io_in:   (once the previous call's input was converted) DMA of the input,
-//            page-locked host int32 -> io_in32
-//   stream:  io_in32 -> current buffer (int8, checked), the sweeps, current
-//            buffer -> io_out32 (once the previous call's output left)
-//   io_out:  DMA of io_out32 -> page-locked host int32
-// The copy engines move one call's input and the previous call's output
-// while the SMs sweep: kernels that read or write host memory directly would
-// hold SMs for the whole transfer and serialise with the sweeps.
+// Pipelined host I/O.  Call k uses staging pair b = k % 2, on three streams:
+//   io_in:   (once call k-2 converted io_in32[b]) DMA of the input,
+//            page-locked host int32 -> io_in32[b]
+//   stream:  io_in32[b] -> current buffer (int8, checked), the sweeps, current
+//            buffer -> io_out32[b] (once call k-2's output left io_out32[b])
+//   io_out:  DMA of io_out32[b] -> page-locked host int32
+// The copy engines move the next calls' inputs and the previous calls'
+// outputs while the SMs sweep, back to back in each direction: the host link
+// (about 210 GB/s one way, 170 GB/s each way with both directions busy on a
+// GB300 host) is the bound of a step whose sweeps take less time than its
+// copies.  Kernels that read or write host memory directly reach the same
+// link rate but hold SMs for the whole transfer.
 static int ens_io_setup(spkgpu_ensemble *e) {
   if (e->io_in) return SPKGPU_OK;
   const size_t bytes = (size_t)e->nsites * sizeof(int32_t);
-  if (cudaMalloc((void **)&e->io_in32, bytes) != cudaSuccess || cudaMalloc((void **)&e->io_out32, bytes) != cudaSuccess)
-    return ens_fail(e, SPKGPU_ERR_NOMEM, "run_io staging buffers");
-  for (cudaEvent_t *ev : {&e->ev_in_ready, &e->ev_in_free, &e->ev_snap_ready, &e->ev_snap_free})
-    ENS_CUDA(e, cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  for (int b = 0; b < 2; b++)
+    if (cudaMalloc((void **)&e->io_in32[b], bytes) != cudaSuccess ||
+        cudaMalloc((void **)&e->io_out32[b], bytes) != cudaSuccess)
+      return ens_fail(e, SPKGPU_ERR_NOMEM, "run_io staging buffers");
+  for (int b = 0; b < 2; b++)
+    for (cudaEvent_t *ev : {&e->ev_in_ready[b], &e->ev_in_free[b], &e->ev_snap_ready[b], &e->ev_snap_free[b]})
+      ENS_CUDA(e, cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
   ENS_CUDA(e, cudaStreamCreateWithFlags(&e->io_in, cudaStreamNonBlocking));
   ENS_CUDA(e, cudaStreamCreateWithFlags(&e->io_out, cudaStreamNonBlocking));
-  ENS_CUDA(e, cudaEventRecord(e->ev_in_free, e->stream));
-  ENS_CUDA(e, cudaEventRecord(e->ev_snap_free, e->stream));
+  for (int b = 0; b < 2; b++) {
+    ENS_CUDA(e, cudaEventRecord(e->ev_in_free[b], e->stream));
+    ENS_CUDA(e, cudaEventRecord(e->ev_snap_free[b], e->stream));
+  }
   return SPKGPU_OK;
 }
 
@@ -1254,26 +1266,28 @@ int spkgpu_ensemble_run_io(spkgpu_ensemble *e, const int32_t *in, int32_t *out, 
   if (rc) return rc;
   const int64_t n = e->nsites;
   const size_t bytes = (size_t)n * sizeof(int32_t);
+  const int b = e->io_calls & 1;
   if (!e->io_pending) {
     ENS_CUDA(e, cudaMemsetAsync(e->d_bad, 0, sizeof(int), e->stream));
     e->io_pending = true;
   }
-  ENS_CUDA(e, cudaStreamWaitEvent(e->io_in, e->ev_in_free, 0));
-  ENS_CUDA(e, cudaMemcpyAsync(e->io_in32, in, bytes, cudaMemcpyHostToDevice, e->io_in));
-  ENS_CUDA(e, cudaEventRecord(e->ev_in_ready, e->io_in));
-  ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->ev_in_ready, 0));
-  ENS_CUDA(e, launch_convert_in(e->spin_bytes, e->io_in32, e->buf[e->parity], n, e->d.nspins, e->d_bad, e->stream));
-  ENS_CUDA(e, cudaEventRecord(e->ev_in_free, e->stream));
+  ENS_CUDA(e, cudaStreamWaitEvent(e->io_in, e->ev_in_free[b], 0));
+  ENS_CUDA(e, cudaMemcpyAsync(e->io_in32[b], in, bytes, cudaMemcpyHostToDevice, e->io_in));
+  ENS_CUDA(e, cudaEventRecord(e->ev_in_ready[b], e->io_in));
+  ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->ev_in_ready[b], 0));
+  ENS_CUDA(e, launch_convert_in(e->spin_bytes, e->io_in32[b], e->buf[e->parity], n, e->d.nspins, e->d_bad, e->stream));
+  ENS_CUDA(e, cudaEventRecord(e->ev_in_free[b], e->stream));
   e->launches += 1;
   rc = ens_enqueue(e, nsweeps);
   if (rc) return rc;
-  ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->ev_snap_free, 0));
-  ENS_CUDA(e, launch_convert_out(e->spin_bytes, e->buf[e->parity], e->io_out32, n, e->stream));
-  ENS_CUDA(e, cudaEventRecord(e->ev_snap_ready, e->stream));
+  ENS_CUDA(e, cudaStreamWaitEvent(e->stream, e->ev_snap_free[b], 0));
+  ENS_CUDA(e, launch_convert_out(e->spin_bytes, e->buf[e->parity], e->io_out32[b], n, e->stream));
+  ENS_CUDA(e, cudaEventRecord(e->ev_snap_ready[b], e->stream));
   e->launches += 1;
-  ENS_CUDA(e, cudaStreamWaitEvent(e->io_out, e->ev_snap_ready, 0));
-  ENS_CUDA(e, cudaMemcpyAsync(out, e->io_out32, bytes, cudaMemcpyDeviceToHost, e->io_out));
-  ENS_CUDA(e, cudaEventRecord(e->ev_snap_free, e->io_out));
+  ENS_CUDA(e, cudaStreamWaitEvent(e->io_out, e->ev_snap_ready[b], 0));
+  ENS_CUDA(e, cudaMemcpyAsync(out, e->io_out32[b], bytes, cudaMemcpyDeviceToHost, e->io_out));
+  ENS_CUDA(e, cudaEventRecord(e->ev_snap_free[b], e->io_out));
+  e->io_calls++;
   return SPKGPU_OK;
 }
 

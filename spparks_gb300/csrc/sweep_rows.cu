@@ -11,10 +11,17 @@
 // not written during the launch, so the order equals the reference's colour
 // order (src/app_lattice.cpp:672-680).
 //
+// Staged rows hold one periodic-image column on each side of the row (so no
+// neighbour index wraps), with the row's first site 16-byte aligned: rows
+// whose length in bytes is a multiple of 16 arrive by 16-byte cp.async.
+//
 // The distinct-value list of potts/neighonly and potts/neigh
-// (src/app_potts_neighonly.cpp:80-88) is built with a 128-bit seen-set in the
-// thread's 16 bytes of shared memory when every value is below 128, else with
-// the pairwise scan.
+// (src/app_potts_neighonly.cpp:80-88) is built, when every value is below
+// 128, with a stamp table: one byte per (value, thread), set to the site's
+// stamp for the site's own value and then for each neighbour in order; a
+// neighbour whose entry did not hold the stamp yet is a first appearance.
+// The unlike counts then compare the neighbour values packed four per word.
+// Larger values take the pairwise scan and per-neighbour compares.
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -25,66 +32,124 @@
 
 namespace spk {
 
-// the value of neighbour j of the site at column x of the centre row, read
-// again from the staged rows (a runtime j: one shared-memory load instead of
-// a select over every neighbour)
-// (sq/8n and sc/26n: every offset in {-1,0,1}^d but 0, dx outer and dz
-// inner, so offset j is cell m = j or j+1 of that cube)
-template <typename S, int LAT>
-__device__ __forceinline__ int staged_neighbor(const S *rows, int nx, int x, int j) {
-  static_assert(LAT == SPKGPU_SQ_8N || LAT == SPKGPU_SC_26N, "row kernel lattices");
-  constexpr int MID = Stencil<LAT>::k3d ? 13 : 4;
-  const int m = j < MID ? j : j + 1;
-  int dx, dy, dz;
-  if (Stencil<LAT>::k3d) {
-    dx = m / 9 - 1;
-    dy = (m / 3) % 3 - 1;
-    dz = m % 3 - 1;
-  } else {
-    dx = m / 3 - 1;
-    dy = m % 3 - 1;
-    dz = 0;
-  }
-  int xn = x + dx;
-  xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
-  const int r = Stencil<LAT>::k3d ? (dz + 1) * 3 + (dy + 1) : dy + 1;
-  return (int)rows[r * nx + xn];
+// elements before a staged row's first site (16 bytes: the image of site
+// nx-1 sits just before it, the image of site 0 just after site nx-1)
+template <typename S>
+__host__ __device__ constexpr int row_lead() {
+  return 16 / (int)sizeof(S);
 }
 
-// first-appearance mask of the distinct values != own among nb[] (values
-// 1..127; first_appearance's result) from a 128-bit seen-set in this
-// thread's four words of shared memory: a load, a test and a store per
-// neighbour
+// staged row r (0..NROWS-1) of neighbour j of the row kernels' stencils:
+// (dz+1)*3 + (dy+1) in 3d, dy+1 in 2d
+template <int LAT>
+__device__ __forceinline__ void row_of_neighbor(int j, int &r, int &dx) {
+  int dy, dz;
+  Stencil<LAT>::offset(j, dx, dy, dz);
+  r = Stencil<LAT>::k3d ? (dz + 1) * 3 + (dy + 1) : dy + 1;
+}
+
+// position of set bit n (0-based, in ascending order) of m; n < popc(m)
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int n) {
+  int pos = 0;
+  int c = __popc(m & 0xFFFFu);
+  if (n >= c) {
+    n -= c;
+    m >>= 16;
+    pos += 16;
+  }
+  c = __popc(m & 0xFFu);
+  if (n >= c) {
+    n -= c;
+    m >>= 8;
+    pos += 8;
+  }
+  c = __popc(m & 0xFu);
+  if (n >= c) {
+    n -= c;
+    m >>= 4;
+    pos += 4;
+  }
+  c = __popc(m & 0x3u);
+  if (n >= c) {
+    n -= c;
+    m >>= 2;
+    pos += 2;
+  }
+  if (n >= (int)(m & 1u)) pos += 1;
+  return pos;
+}
+
+// neighbour values below 128 packed four per word (bytes, neighbour order);
+// the unused lanes of the last word hold 0, which no site value equals
 template <int NN>
-__device__ __forceinline__ uint32_t first_appearance_shared(int own, const int (&nb)[NN], uint32_t *seen) {
-  *(uint4 *)seen = make_uint4(0u, 0u, 0u, 0u);
-  seen[own >> 5] = 1u << (own & 31);
+struct PackedNb {
+  static constexpr int NW = (NN + 3) / 4;
+  uint32_t w[NW];
+};
+
+template <int NN>
+__device__ __forceinline__ PackedNb<NN> pack_neighbors(const int (&nb)[NN]) {
+  PackedNb<NN> p;
+#pragma unroll
+  for (int k = 0; k < PackedNb<NN>::NW; k++) {
+    const int j = 4 * k;
+    // byte 1 of a value below 128 is 0: selector 1 fills the empty lanes
+    const uint32_t lo = __byte_perm((uint32_t)nb[j], j + 1 < NN ? (uint32_t)nb[j + 1] : 0u, 0x1140u);
+    const uint32_t hi = j + 2 < NN ? __byte_perm((uint32_t)nb[j + 2], j + 3 < NN ? (uint32_t)nb[j + 3] : 0u, 0x1140u)
+                                   : 0u;
+    p.w[k] = __byte_perm(lo, hi, 0x5410u);
+  }
+  return p;
+}
+
+// neighbours whose value differs from v (1..127): per byte lane, (b ^ v) is
+// below 128, so adding 0x7F sets bit 7 exactly where it is non-zero and never
+// carries into the next lane
+template <int NN>
+__device__ __forceinline__ int unlike_packed(const PackedNb<NN> &p, int v) {
+  const uint32_t vv = (uint32_t)v * 0x01010101u;
+  uint32_t acc = 0;
+#pragma unroll
+  for (int k = 0; k < PackedNb<NN>::NW; k++) acc += (((p.w[k] ^ vv) + 0x7F7F7F7Fu) & 0x80808080u) >> 7;
+  return (int)((acc * 0x01010101u) >> 24) - (4 * PackedNb<NN>::NW - NN);  // empty lanes differ from every v
+}
+
+// first_appearance's result from the stamp table: tab + v * row_bytes is
+// this thread's byte for value v
+template <int NN>
+__device__ __forceinline__ uint32_t first_appearance_stamped(int own, const int (&nb)[NN], unsigned char *tab,
+                                                             int row_bytes, unsigned char stamp) {
+  tab[own * row_bytes] = stamp;
   uint32_t first = 0;
 #pragma unroll
   for (int j = 0; j < NN; j++) {
-    const int v = nb[j];
-    const uint32_t b = 1u << (v & 31);
-    const uint32_t cur = seen[v >> 5];
-    first |= ((cur & b) ? 0u : 1u) << j;
-    seen[v >> 5] = cur | b;
+    unsigned char *e = tab + nb[j] * row_bytes;
+    if (*e != stamp) first |= 1u << j;
+    *e = stamp;
   }
   return first;
 }
 
+// the site's new value (src/app_ising.cpp:104-136, src/app_potts.cpp:112-146,
+// src/app_potts_neighonly.cpp:71-117); pick_offset[j] is the staged-row
+// offset of neighbour j from the site's position in row 0
 template <typename S, int LAT, int APP, bool SMALLQ>
 __device__ __forceinline__ int update_rows(int own, const int (&nb)[Stencil<LAT>::NN], uint32_t x0, uint32_t x1,
-                                           int nspins, const uint64_t *thr, const S *rows, int nx, int x,
-                                           uint32_t *seen) {
+                                           int nspins, const uint64_t *thr, const S *site0, const int *pick_offset,
+                                           unsigned char *tab, int row_bytes, unsigned char stamp) {
   constexpr int NN = Stencil<LAT>::NN;
   if (APP == SPKGPU_ISING || APP == SPKGPU_POTTS) {
     int e0;
     return update_philox<NN, APP>(own, nb, x0, x1, nspins, thr, &e0);
   }
-  int e0 = count_unlike<NN>(own, nb);
+  PackedNb<NN> pk;
+  if (SMALLQ) pk = pack_neighbors<NN>(nb);
+  const int e0 = SMALLQ ? unlike_packed<NN>(pk, own) : count_unlike<NN>(own, nb);
   // no unlike neighbour: no event and no draw (nevent == 0 below)
   if (e0 == 0) return own;
-  uint32_t first = SMALLQ ? first_appearance_shared<NN>(own, nb, seen) : first_appearance<NN>(own, nb);
-  int nevent = __popc(first);
+  const uint32_t first =
+      SMALLQ ? first_appearance_stamped<NN>(own, nb, tab, row_bytes, stamp) : first_appearance<NN>(own, nb);
+  const int nevent = __popc(first);
   uint32_t iran;
   if (APP == SPKGPU_POTTS_NEIGHONLY) {
     if (nevent == 0) return own;
@@ -94,8 +159,8 @@ __device__ __forceinline__ int update_rows(int own, const int (&nb)[Stencil<LAT>
     iran = scaled_pick((uint32_t)NN, x0);
     if ((int)iran >= nevent) return own;
   }
-  int news = staged_neighbor<S, LAT>(rows, nx, x, __fns(first, 0, (int)iran + 1));
-  int e1 = count_unlike<NN>(news, nb);
+  const int news = (int)site0[pick_offset[nth_set_bit(first, (int)iran)]];
+  const int e1 = SMALLQ ? unlike_packed<NN>(pk, news) : count_unlike<NN>(news, nb);
   if (e1 <= e0) return news;
   return ((uint64_t)x1 < thr[e1 - e0]) ? news : own;  // thr is all 0 at zero temperature
 }
@@ -110,71 +175,140 @@ struct RowArgs {
   AcceptTable acc;
 };
 
-// rows staged: index (dz+1)*3 + (dy+1) for 3d, (dy+1) for 2d
+// the stamp table of the distinct-value list: apps that build one, values below 128
+template <int APP, bool SMALLQ>
+__host__ __device__ constexpr bool row_stamps() {
+  return SMALLQ && (APP == SPKGPU_POTTS_NEIGHONLY || APP == SPKGPU_POTTS_NEIGH);
+}
+
+// staged row pitch in elements: the row rounded up to 16 bytes plus a lead
+// on each side, so every staged row starts at a multiple of 16 bytes
+template <typename S>
+__host__ __device__ __forceinline__ int row_pitch(int nx) {
+  constexpr int LEAD = row_lead<S>();
+  return (nx + LEAD - 1) / LEAD * LEAD + 2 * LEAD;
+}
+
+// bytes per value row of the stamp table: one per thread, in groups of four
+// warps
+__host__ __device__ __forceinline__ int stamp_row_bytes(int threads) { return (threads + 127) / 128 * 128; }
+
+// shared memory of row_pair_kernel: the staged rows, then the stamp table
+// ((nspins + 1) value rows)
+template <typename S, int LAT>
+inline size_t row_pair_smem(int nx, int threads, int nspins, bool stamps) {
+  constexpr int NROWS = Stencil<LAT>::k3d ? 9 : 3;
+  const size_t rows = (size_t)NROWS * row_pitch<S>(nx) * sizeof(S);
+  const size_t tab = stamps ? (size_t)(nspins + 1) * stamp_row_bytes(threads) : 0;
+  return rows + tab;
+}
+
 template <typename S, int LAT, int APP, bool SMALLQ>
 __global__ void __launch_bounds__(512) row_pair_kernel(RowArgs a) {
   constexpr int NN = Stencil<LAT>::NN;
   constexpr int NROWS = Stencil<LAT>::k3d ? 9 : 3;
+  constexpr int LEAD = row_lead<S>();
+  constexpr bool STAMPS = row_stamps<APP, SMALLQ>();
   extern __shared__ __align__(16) unsigned char row_smem[];
-  S *rows = (S *)row_smem;
-  // 16 bytes of seen-set per thread after the rows (16-byte aligned)
-  const size_t rows_bytes = ((size_t)NROWS * a.nx * sizeof(S) + 15) & ~(size_t)15;
-  uint32_t *seen = (uint32_t *)(row_smem + rows_bytes) + 4 * threadIdx.x;
-  __shared__ uint64_t thr[kMaxNeigh + 1];
-  if (threadIdx.x <= kMaxNeigh) thr[threadIdx.x] = a.acc.thr[threadIdx.x];
   const int nx = a.nx;
+  const int pitch = row_pitch<S>(nx);
+  S *rows = (S *)row_smem;
+  const size_t rows_bytes = (size_t)NROWS * pitch * sizeof(S);  // a multiple of 16
+  const int t = threadIdx.x;
+  // stamp table: value row v holds one byte per thread; the 32 lanes of a
+  // warp use 32 distinct words of a row (no bank conflicts), four warps
+  // share those words
+  const int row_bytes = stamp_row_bytes(blockDim.x);
+  unsigned char *tab = row_smem + rows_bytes + (t >> 7) * 128 + (t & 31) * 4 + ((t >> 5) & 3);
+  if (STAMPS) {
+    uint4 *z = (uint4 *)(row_smem + rows_bytes);
+    const int n16 = (a.nspins + 1) * row_bytes / 16;
+    for (int k = t; k < n16; k += blockDim.x) z[k] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __shared__ uint64_t thr[kMaxNeigh + 1];
+  __shared__ int pick_offset[NN];  // staged offset of neighbour j from the site's position in row 0
+  if (t <= kMaxNeigh) thr[t] = a.acc.thr[t];
+  if (t < NN) {
+    int r, dx;
+    row_of_neighbor<LAT>(t, r, dx);
+    pick_offset[t] = r * pitch + dx;
+  }
   // this CTA's row
-  int rows_y = (a.ny - a.qy + 1) / 2;
-  int iy = blockIdx.x % rows_y, iz = blockIdx.x / rows_y;
-  int y = 2 * iy + a.qy;
-  int z = Stencil<LAT>::k3d ? 2 * iz + a.qz : 0;
+  const int rows_y = (a.ny - a.qy + 1) / 2;
+  const int iy = blockIdx.x % rows_y, iz = blockIdx.x / rows_y;
+  const int y = 2 * iy + a.qy;
+  const int z = Stencil<LAT>::k3d ? 2 * iz + a.qz : 0;
   S *spin = (S *)a.spin;
-  for (int r = 0; r < NROWS; r++) {
-    int dy = Stencil<LAT>::k3d ? (r % 3) - 1 : r - 1;
-    int dz = Stencil<LAT>::k3d ? (r / 3) - 1 : 0;
+  // the lattice row of staged row r
+  auto row_src = [&](int r) {
+    const int dy = Stencil<LAT>::k3d ? (r % 3) - 1 : r - 1;
+    const int dz = Stencil<LAT>::k3d ? (r / 3) - 1 : 0;
     int yy = y + dy, zz = z + dz;
     yy = yy < 0 ? yy + a.ny : (yy >= a.ny ? yy - a.ny : yy);
     if (Stencil<LAT>::k3d) zz = zz < 0 ? zz + a.nz : (zz >= a.nz ? zz - a.nz : zz);
-    const S *src = spin + ((int64_t)zz * a.ny + yy) * nx;
-    for (int x = threadIdx.x; x < nx; x += blockDim.x) rows[r * nx + x] = src[x];
+    return (const S *)(spin + ((int64_t)zz * a.ny + yy) * nx);
+  };
+  if ((nx * (int)sizeof(S)) % 16 == 0 && ((uintptr_t)spin & 15) == 0) {
+    // 16-byte copies (rows of the lattice start at multiples of 16 bytes)
+    const int cpr = nx / LEAD;  // chunks per row
+    for (int k = t; k < NROWS * cpr; k += blockDim.x) {
+      const int r = k / cpr, c = k - r * cpr;
+      const unsigned sa = (unsigned)__cvta_generic_to_shared(rows + r * pitch + LEAD + c * LEAD);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(row_src(r) + c * LEAD) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  } else {
+    for (int r = 0; r < NROWS; r++) {
+      const S *src = row_src(r);
+      for (int x = t; x < nx; x += blockDim.x) rows[r * pitch + LEAD + x] = src[x];
+    }
   }
   __syncthreads();
-  const int center = Stencil<LAT>::k3d ? 4 : 1;
+  if (t < 2 * NROWS) {  // the periodic images beside each row
+    S *row = rows + (t >> 1) * pitch + LEAD;
+    if (t & 1) row[nx] = row[0];
+    else row[-1] = row[nx - 1];
+  }
+  __syncthreads();
   const int64_t rowbase = ((int64_t)z * a.ny + y) * nx;
   unsigned int changed = 0;
   const RoundKeys rk = round_keys(a.seed, kStreamSweep);
   // thread p owns the pair (2p, 2p+1); blockDim.x >= nx/2
-  const int p = threadIdx.x;
+  const int p = t;
   const bool active = 2 * p < nx;
   uint32_t keep0 = 0, keep1 = 0;
+  const int crow = (NROWS / 2) * pitch + LEAD;  // the centre row's first site
 #pragma unroll
   for (int half = 0; half < 2; half++) {
     if (active) {
-      int x = 2 * p + half;
+      const int x = 2 * p + half;
       uint32_t x0, x1;
       if (half == 0) {
-        int64_t s = rowbase + 2 * p;
-        U4 w = philox4x32_10_rk(sweep_counter<APP>((uint64_t)s, a.sweep, 0u), rk);
+        const int64_t s = rowbase + 2 * p;
+        const U4 w = philox4x32_10_rk(sweep_counter<APP>((uint64_t)s, a.sweep, 0u), rk);
         site_words<APP>(w, (uint64_t)s, x0, x1);
         site_words<APP>(w, (uint64_t)s + 1, keep0, keep1);
       } else {
         x0 = keep0;
         x1 = keep1;
       }
+      const S *site0 = rows + LEAD + x;  // the site's position in staged row 0
       int nb[NN];
 #pragma unroll
       for (int j = 0; j < NN; j++) {
-        int dx, dy, dz;
-        Stencil<LAT>::offset(j, dx, dy, dz);
-        int xn = x + dx;
-        xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
-        int r = Stencil<LAT>::k3d ? (dz + 1) * 3 + (dy + 1) : dy + 1;
-        nb[j] = rows[r * nx + xn];
+        int r, dx;
+        row_of_neighbor<LAT>(j, r, dx);
+        nb[j] = site0[r * pitch + dx];
       }
-      int own = rows[center * nx + x];
-      int news = update_rows<S, LAT, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr, rows, nx, x, seen);
+      const int own = rows[crow + x];
+      const int news = update_rows<S, LAT, APP, SMALLQ>(own, nb, x0, x1, a.nspins, thr, site0, pick_offset, tab,
+                                                        row_bytes, (unsigned char)(half + 1));
       if (news != own) {
-        rows[center * nx + x] = (S)news;
+        rows[crow + x] = (S)news;
+        // the images of sites 0 and nx-1 beside the centre row
+        if (x == 0) rows[crow + nx] = (S)news;
+        if (x == nx - 1) rows[crow - 1] = (S)news;
         spin[rowbase + x] = (S)news;
         changed++;
       }
@@ -196,7 +330,8 @@ static cudaError_t launch_rows_app(const RowArgs &a, bool smallq, cudaStream_t s
   int rows_z = Stencil<LAT>::k3d ? (a.nz - a.qz + 1) / 2 : 1;
   unsigned grid = (unsigned)(rows_y * rows_z);
   int threads = ((a.nx / 2 + 31) / 32) * 32;  // one x-pair per thread
-  size_t smem = (((size_t)NROWS * a.nx * sizeof(S) + 15) & ~(size_t)15) + (size_t)threads * 16;
+  const bool stamps = smallq && (APP == SPKGPU_POTTS_NEIGHONLY || APP == SPKGPU_POTTS_NEIGH);
+  const size_t smem = row_pair_smem<S, LAT>(a.nx, threads, a.nspins, stamps);
   if (smallq) {
     auto f = row_pair_kernel<S, LAT, APP, true>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

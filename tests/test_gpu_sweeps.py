@@ -113,6 +113,47 @@ def test_random_cases_match_oracle(sg, case, variant):
     assert (st["naccept"], st["nattempt"]) == (na, nt)
 
 
+# the row-pair kernel (sq/8n and sc/26n without sectors): stamp table and
+# packed counts for potts/neighonly and potts/neigh with values below 128,
+# the pairwise scan above; 16-byte staged copies where a row's bytes are a
+# multiple of 16, element copies elsewhere; one to sixteen warps per row
+ROW_CASES = [
+    dict(lattice="sc/26n", nx=16, ny=6, nz=4, app="potts/neighonly", nspins=20, temperature=0.5, sb=1),
+    dict(lattice="sc/26n", nx=24, ny=4, nz=6, app="potts/neighonly", nspins=100, temperature=0.5, sb=2),
+    dict(lattice="sc/26n", nx=20, ny=4, nz=4, app="potts/neigh", nspins=9, temperature=0.9, sb=1),
+    dict(lattice="sc/26n", nx=10, ny=6, nz=4, app="potts/neighonly", nspins=300, temperature=0.7, sb=2),
+    dict(lattice="sc/26n", nx=12, ny=4, nz=4, app="potts/neighonly", nspins=127, temperature=0.0, sb=4),
+    dict(lattice="sq/8n", nx=300, ny=6, nz=1, app="potts/neighonly", nspins=127, temperature=0.6, sb=4),
+    dict(lattice="sq/8n", nx=1024, ny=4, nz=1, app="potts/neighonly", nspins=50, temperature=0.8, sb=2),
+    dict(lattice="sq/8n", nx=18, ny=8, nz=1, app="potts", nspins=5, temperature=0.8, sb=1),
+    dict(lattice="sq/8n", nx=32, ny=8, nz=1, app="ising", nspins=2, temperature=1.5, sb=2),
+    dict(lattice="sq/8n", nx=64, ny=4, nz=1, app="potts/neigh", nspins=30, temperature=0.4, sb=1),
+]
+
+
+@pytest.mark.parametrize("case", ROW_CASES,
+                         ids=lambda c: f"{c['app']}-{c['lattice']}-{c['nx']}-Q{c['nspins']}-int{8 * c['sb']}")
+def test_row_pair_kernel_matches_oracle(sg, case):
+    seed = 8642
+    n = case["nx"] * case["ny"] * case["nz"]
+    spin = oracle.init_spins(seed, n, 1, case["nspins"])
+    cfg = oracle.make_cfg(case["lattice"], case["nx"], case["ny"], case["nz"], case["app"], case["nspins"],
+                          case["temperature"], 1, 1, 0, seed)
+    ref = spin.copy()
+    na, nt, hashes = oracle.color_sweeps(cfg, ref, 0, 4)
+    lat = sg.Lattice(case["lattice"], case["nx"], case["ny"], case["nz"], case["app"], case["nspins"],
+                     spin_bytes=case["sb"], seed=seed, variant=0)
+    lat.set_temperature(case["temperature"])
+    lat.upload(spin)
+    got = []
+    for s in range(4):
+        lat.sweep(1)
+        got.append(oracle.spin_hash(lat.download()))
+    assert got == [int(h) for h in hashes]
+    assert (lat.stats()["naccept"], lat.stats()["nattempt"]) == (na, nt)
+    lat.close()
+
+
 @pytest.mark.parametrize("procs,nsector", [((2, 2, 1), 4), ((3, 1, 1), 2), ((2, 1, 1), 1)])
 def test_processor_grid_sectors_match_oracle(sg, procs, nsector):
     """`processors Px Py 1` + `sector`: sector k of every sub-domain is one set
