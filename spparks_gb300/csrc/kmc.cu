@@ -475,6 +475,14 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
   const int lwx = __ffs(wx) - 1, lwy = __ffs(wy) - 1;
 
   for (int p = lane; p < ntop; p += 32) cp_async8(top + p, G + p);
+  // the Boltzmann factors in shared memory: lanes index them with different
+  // energy changes, which an indexed parameter load would serialise
+  __shared__ double s_pexp[kMaxNeigh + 1];
+  __shared__ float s_pexpf[kMaxNeigh + 1];
+  if (lane <= kMaxNeigh) {
+    s_pexp[lane] = a.zero_t ? 0.0 : a.pexp[lane];
+    s_pexpf[lane] = a.zero_t ? 0.0f : a.pexpf[lane];
+  }
   // this lane's changed site: 0 = the event site, j = neighbour j-1
   int odx = 0, ody = 0, odz = 0;
   if (lane >= 1 && lane <= NN) St::offset(lane - 1, odx, ody, odz);
@@ -691,33 +699,34 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
         const int e1 = count_unlike<NN>(mv, nb);
         const bool live = lane < NN && ((first >> lane) & 1u);
         int val = own;
-        bool found = false;
+        // the running sum stops at the first value that reaches the
+        // threshold (the same on every lane: a uniform branch)
         if (a.fp64) {
-          const double term = !live ? 0.0 : (e1 <= e0 ? 1.0 : (a.zero_t ? 0.0 : a.pexp[e1 - e0]));
+          const double term = !live ? 0.0 : (e1 <= e0 ? 1.0 : s_pexp[e1 - e0]);
           double tj[NN];
 #pragma unroll
           for (int j = 0; j < NN; j++) tj[j] = __shfl_sync(FULL, term, j);
           double prob = 0.0;
 #pragma unroll
           for (int j = 0; j < NN; j++) {
-            if (!found && ((first >> j) & 1u)) {
+            if ((first >> j) & 1u) {
               prob += tj[j];
               val = nb[j];
-              found = nonneg_le(threshhold, prob);  // prob >= threshhold
+              if (nonneg_le(threshhold, prob)) break;  // prob >= threshhold
             }
           }
         } else {
-          const float term = !live ? 0.0f : (e1 <= e0 ? 1.0f : (a.zero_t ? 0.0f : a.pexpf[e1 - e0]));
+          const float term = !live ? 0.0f : (e1 <= e0 ? 1.0f : s_pexpf[e1 - e0]);
           float tj[NN];
 #pragma unroll
           for (int j = 0; j < NN; j++) tj[j] = __shfl_sync(FULL, term, j);
           float prob = 0.0f;
 #pragma unroll
           for (int j = 0; j < NN; j++) {
-            if (!found && ((first >> j) & 1u)) {
+            if ((first >> j) & 1u) {
               prob += tj[j];
               val = nb[j];
-              found = nonneg_le(threshhold, (double)prob);
+              if (nonneg_le(threshhold, (double)prob)) break;
             }
           }
         }
@@ -746,7 +755,7 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
       const int e0 = count_unlike<NN>(own, nb);
       if (APP == SPKGPU_ISING) {
         const int e1 = count_unlike<NN>(own == 1 ? 2 : 1, nb);
-        p = e1 <= e0 ? 1.0 : (a.zero_t ? 0.0 : (a.fp64 ? a.pexp[e1 - e0] : (double)a.pexpf[e1 - e0]));
+        p = e1 <= e0 ? 1.0 : (a.fp64 ? s_pexp[e1 - e0] : (double)s_pexpf[e1 - e0]);
       } else {
         const uint32_t first = first_appearance<NN>(own, nb);
         if (a.fp64) {
@@ -755,7 +764,7 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
             if (!((first >> j) & 1u)) continue;
             const int e1 = count_unlike<NN>(nb[j], nb);
             if (e1 <= e0) p += 1.0;
-            else if (!a.zero_t) p += a.pexp[e1 - e0];
+            else if (!a.zero_t) p += s_pexp[e1 - e0];
           }
         } else {
           float pf = 0.0f;
@@ -764,7 +773,7 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
             if (!((first >> j) & 1u)) continue;
             const int e1 = count_unlike<NN>(nb[j], nb);
             if (e1 <= e0) pf += 1.0f;
-            else if (!a.zero_t) pf += a.pexpf[e1 - e0];
+            else if (!a.zero_t) pf += s_pexpf[e1 - e0];
           }
           p = (double)pf;
         }
