@@ -443,6 +443,48 @@ __device__ __forceinline__ void load_slot(const double *G, double *S, int A, int
   }
 }
 
+// SolveTree::find (src/solve_tree.cpp:207-224) over `levels` levels of the
+// heap T rooted at index 0 (children of u at 2u+1, 2u+2): returns the index
+// reached and leaves the remaining value in `value`, bit for bit as the
+// reference's walk.  Two levels per step: the left child and both
+// grandchildren that can come next are read together, then the two
+// decisions are taken in turn.  The walk is the same on every lane (no
+// divergence, no broadcast afterwards).  Branch-free forms (the subtraction
+// always issued, the compare selecting) and FP64 compares measured slower.
+__device__ __forceinline__ int heap_walk(const double *T, int levels, double &value) {
+  int u = 0;
+  for (; levels >= 2; levels -= 2) {
+    const int l = 2 * u + 1;
+    const double tl = T[l], tll = T[2 * l + 1], trl = T[2 * l + 3];
+    if (nonneg_le(value, tl)) {
+      u = l;
+      if (nonneg_le(value, tll)) u = 2 * l + 1;
+      else {
+        value -= tll;
+        u = 2 * l + 2;
+      }
+    } else {
+      value -= tl;
+      u = l + 1;
+      if (nonneg_le(value, trl)) u = 2 * l + 3;
+      else {
+        value -= trl;
+        u = 2 * l + 4;
+      }
+    }
+  }
+  if (levels) {
+    const int l = 2 * u + 1;
+    const double tl = T[l];
+    if (nonneg_le(value, tl)) u = l;
+    else {
+      value -= tl;
+      u = l + 1;
+    }
+  }
+  return u;
+}
+
 template <typename S, int LAT, int APP>
 __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset) {
   using St = Stencil<LAT>;
@@ -527,84 +569,18 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
     // the clock step does not depend on the pick (SolveTree::event,
     // src/solve_tree.cpp:130-143)
     const double dt = -1.0 / sum * lu;
-    // SolveTree::find through the cached levels (src/solve_tree.cpp:207-224)
-    // every lane walks (the same loads and decisions on every lane: no
-    // divergence, no broadcast afterwards)
-    // Two levels per step: the left child and both grandchildren that can
-    // come next are read together, then the two decisions are taken in turn.
-    int node = 0;
+    // SolveTree::find (src/solve_tree.cpp:207-224): through the cached
+    // levels, then (below level 13) through the picked level-13 node's
+    // descendants, fetched in one round trip; every lane walks
     double value = ux * sum;
-    {
-      int steps = whole ? depth : kTopLevels - 1;  // down to the leaves or to level 13
-      for (; steps >= 2; steps -= 2) {
-        const int l = 2 * node + 1;
-        const double tl = top[l], tll = top[2 * l + 1], trl = top[2 * l + 3];
-        if (nonneg_le(value, tl)) {
-          node = l;
-          if (nonneg_le(value, tll)) node = 2 * l + 1;
-          else {
-            value -= tll;
-            node = 2 * l + 2;
-          }
-        } else {
-          value -= tl;
-          node = l + 1;
-          if (nonneg_le(value, trl)) node = 2 * l + 3;
-          else {
-            value -= trl;
-            node = 2 * l + 4;
-          }
-        }
-      }
-      if (steps) {
-        const int l = 2 * node + 1;
-        const double tl = top[l];
-        if (nonneg_le(value, tl)) node = l;
-        else {
-          value -= tl;
-          node = l + 1;
-        }
-      }
-    }
+    int node = heap_walk(top, whole ? depth : kTopLevels - 1, value);
     double *SF = slots + (size_t)(NSLOT - 1) * slotn;  // the pick's slot
     if (!whole) {
-      // node is the level-13 node A: its descendants in one round trip
       load_slot(G, SF, node, slotn, lane);
       cp_async_wait_all();
       __syncwarp();
-      const int A = node;
-      int j = 0;  // depth of node below A
-      for (; j + 2 <= hb; j += 2) {
-        const int l = 2 * node + 1;
-        const int tl_at = l - (A << (j + 1)) - 1;
-        const int g0 = 2 * l + 1 - (A << (j + 2)) - 1;  // left child of l; +2: left child of l + 1
-        const double tl = SF[tl_at], tll = SF[g0], trl = SF[g0 + 2];
-        if (nonneg_le(value, tl)) {
-          node = l;
-          if (nonneg_le(value, tll)) node = 2 * l + 1;
-          else {
-            value -= tll;
-            node = 2 * l + 2;
-          }
-        } else {
-          value -= tl;
-          node = l + 1;
-          if (nonneg_le(value, trl)) node = 2 * l + 3;
-          else {
-            value -= trl;
-            node = 2 * l + 4;
-          }
-        }
-      }
-      if (j < hb) {
-        const int l = 2 * node + 1;
-        const double tl = SF[l - (A << (j + 1)) - 1];
-        if (nonneg_le(value, tl)) node = l;
-        else {
-          value -= tl;
-          node = l + 1;
-        }
-      }
+      // slot t holds the descendant at local heap index t + 1
+      node = heap_walk(SF - 1, hb, value) + (node << hb);
     }
     const int m = node - leaf0;
     timesector += dt;
@@ -757,24 +733,45 @@ __global__ void __launch_bounds__(32) kmc_tree_event_kernel(KmcArgs a, int iset)
         const int e1 = count_unlike<NN>(own == 1 ? 2 : 1, nb);
         p = e1 <= e0 ? 1.0 : (a.fp64 ? s_pexp[e1 - e0] : (double)s_pexpf[e1 - e0]);
       } else {
-        const uint32_t first = first_appearance<NN>(own, nb);
+        // one pass over the neighbour pairs gives the first appearances and
+        // each value's multiplicity (its unlike count is NN minus that);
+        // the terms are then added in neighbour order, a value that is not a
+        // first appearance adding 0 (p + 0 == p for p >= 0)
+        uint32_t first = 0;
+        int mult[NN];
+#pragma unroll
+        for (int j = 0; j < NN; j++) mult[j] = 1;
+#pragma unroll
+        for (int j = 0; j < NN; j++) {
+          bool f = nb[j] != own;
+#pragma unroll
+          for (int q = 0; q < j; q++) {
+            const bool eq = nb[q] == nb[j];
+            f = f && !eq;
+            mult[j] += eq;
+            mult[q] += eq;
+          }
+          first |= (f ? 1u : 0u) << j;
+        }
         if (a.fp64) {
+          double t[NN];
 #pragma unroll
           for (int j = 0; j < NN; j++) {
-            if (!((first >> j) & 1u)) continue;
-            const int e1 = count_unlike<NN>(nb[j], nb);
-            if (e1 <= e0) p += 1.0;
-            else if (!a.zero_t) p += s_pexp[e1 - e0];
+            const int e1 = NN - mult[j];
+            t[j] = !((first >> j) & 1u) ? 0.0 : (e1 <= e0 ? 1.0 : s_pexp[max(e1 - e0, 0)]);
           }
+#pragma unroll
+          for (int j = 0; j < NN; j++) p += t[j];
         } else {
+          float t[NN];
+#pragma unroll
+          for (int j = 0; j < NN; j++) {
+            const int e1 = NN - mult[j];
+            t[j] = !((first >> j) & 1u) ? 0.0f : (e1 <= e0 ? 1.0f : s_pexpf[max(e1 - e0, 0)]);
+          }
           float pf = 0.0f;
 #pragma unroll
-          for (int j = 0; j < NN; j++) {
-            if (!((first >> j) & 1u)) continue;
-            const int e1 = count_unlike<NN>(nb[j], nb);
-            if (e1 <= e0) pf += 1.0f;
-            else if (!a.zero_t) pf += s_pexpf[e1 - e0];
-          }
+          for (int j = 0; j < NN; j++) pf += t[j];
           p = (double)pf;
         }
       }
