@@ -736,6 +736,13 @@ def kernel_case(name):
         lat.init_spins(1, 100)
         lat.sweep(2)
         print("rows", lat.stats())
+    elif name == "c0":  # sq/4n Ising 128^2 int32, 100 sweeps in one call (the cluster-resident sweep)
+        lat = sg.Lattice("sq/4n", 128, 128, 1, "ising", 2, spin_bytes=4, seed=5)
+        lat.set_temperature(2.269)
+        lat.init_spins(1, 2)
+        lat.sweep(100)
+        lat.sweep(100)
+        print("c0", lat.stats())
     elif name == "packed":  # bit-packed Ising sc/6n 512^3
         lat = sg.Lattice("sc/6n", 512, 512, 512, "ising", 2, spin_bytes=-1, seed=5)
         lat.set_temperature(4.5115)
@@ -787,7 +794,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--kernel-case", choices=["ensemble", "fused", "rows", "packed", "kmc", "kmc_serial", "rates", "c3"],
+    ap.add_argument("--kernel-case", choices=["ensemble", "fused", "rows", "c0", "packed", "kmc", "kmc_serial", "rates",
+                                              "c3"],
                     help="run one small profiling workload instead of the benchmark")
     args = ap.parse_args()
     if args.kernel_case:
