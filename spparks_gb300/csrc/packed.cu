@@ -7,16 +7,20 @@
 // Per sweep:
 //   packed_draw_kernel   one thread per word computes the Philox blocks of
 //                        its 64 sites (16 blocks, four sites each) once and
-//                        stores four decision masks: the proposal (a site
-//                        word x >= 2^31 proposes value 2) and "y < thr[dE]"
-//                        (y = x & 0x7FFFFFFF) for the three uphill moves
-//                        dE = 2, 4, 6; each bit is a 32-bit compare and a
-//                        predicated OR.
+//                        stores three decision masks: the proposal (a site
+//                        word x >= 2^31 proposes value 2) and the level of
+//                        y = x & 0x7FFFFFFF among the thresholds of the
+//                        three uphill moves dE = 2, 4, 6 (t2 >= t4 >= t6) as
+//                        two bit planes: hi = [y < t4], lo = [y < t6] where
+//                        hi is set and [y < t2] where it is not.  Then
+//                        [y < t2] = hi | lo, [y < t4] = hi and
+//                        [y < t6] = hi & lo.  A site takes two compares, one
+//                        select and three predicated ORs.
 //   packed_phase_kernel  per colour, one thread per word: the unlike count of
 //                        every site against its six neighbours as a
 //                        bit-sliced 3-bit sum of XOR masks; a site of the
 //                        colour flips when its proposal differs from it and
-//                        e0 >= 3 (dE <= 0) or the stored decision for
+//                        e0 >= 3 (dE <= 0) or the decision for
 //                        dE = 6 - 2*e0 holds.  Words are updated in place:
 //                        a colour's bits never neighbour each other, so
 //                        concurrent readers only use bits that do not change.
@@ -30,9 +34,14 @@
 
 namespace spk {
 
-struct PackedDecisions {
-  uint64_t prop, a2, a4, a6;
+// the three decision planes of nw words, one array each (coalesced loads)
+struct PackedPlanes {
+  uint64_t *prop, *hi, *lo;
 };
+__host__ __device__ inline PackedPlanes packed_planes(void *decisions, int64_t nw) {
+  uint64_t *d = (uint64_t *)decisions;
+  return PackedPlanes{d, d + nw, d + 2 * nw};
+}
 
 // c | BIT if x >= 2^31 (the site's word proposes value 2), as a compare and
 // a predicated OR of an immediate
@@ -53,9 +62,9 @@ __device__ __forceinline__ uint32_t or_if_below(uint32_t c, uint32_t x, uint32_t
   return c;
 }
 
-// the four decision masks of a word, as 32-bit halves (index 0: bits 0-31)
+// the three decision planes of a word, as 32-bit halves (index 0: bits 0-31)
 struct PackedHalves {
-  uint32_t prop[2], a2[2], a4[2], a6[2];
+  uint32_t prop[2], hi[2], lo[2];
 };
 
 // the decision bits BIT of one site with Philox word x
@@ -63,9 +72,9 @@ template <uint32_t BIT, int H>
 __device__ __forceinline__ void packed_site(PackedHalves &h, uint32_t x, uint32_t t2, uint32_t t4, uint32_t t6) {
   h.prop[H] = or_if_prop2<BIT>(h.prop[H], x);
   const uint32_t y = x & kIsingAcceptMask;
-  h.a2[H] = or_if_below<BIT>(h.a2[H], y, t2);
-  h.a4[H] = or_if_below<BIT>(h.a4[H], y, t4);
-  h.a6[H] = or_if_below<BIT>(h.a6[H], y, t6);
+  const bool below4 = y < t4;
+  if (below4) h.hi[H] |= BIT;
+  h.lo[H] = or_if_below<BIT>(h.lo[H], y, below4 ? t6 : t2);
 }
 
 // block M (sites 4M .. 4M+3 of the word) and the blocks after it; the block
@@ -98,17 +107,18 @@ __global__ void __launch_bounds__(256, 4) packed_draw_kernel(const PackedArgs a)
     const int64_t s0 = row * a.nx + ((t - row * words_per_row) << 6);  // site of bit 0
     PackedHalves h = {};
     packed_blocks<0>(ising_counter((uint64_t)s0, a.sweep, 0u), rk, t2, t4, t6, h);
-    PackedDecisions *D = (PackedDecisions *)a.decisions;
-    D[t] = PackedDecisions{(uint64_t)h.prop[1] << 32 | h.prop[0], (uint64_t)h.a2[1] << 32 | h.a2[0],
-                           (uint64_t)h.a4[1] << 32 | h.a4[0], (uint64_t)h.a6[1] << 32 | h.a6[0]};
+    const PackedPlanes D = packed_planes(a.decisions, nw);
+    D.prop[t] = (uint64_t)h.prop[1] << 32 | h.prop[0];
+    D.hi[t] = (uint64_t)h.hi[1] << 32 | h.hi[0];
+    D.lo[t] = (uint64_t)h.lo[1] << 32 | h.lo[0];
   }
 }
 
 __global__ void packed_phase_kernel(const PackedArgs a, int color) {
   uint64_t *W = (uint64_t *)a.words;
-  const PackedDecisions *D = (const PackedDecisions *)a.decisions;
   int64_t words_per_row = a.nx >> 6;
   int64_t nw = a.nwords;
+  const PackedPlanes D = packed_planes(a.decisions, nw);
   unsigned long long flips = 0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nw; t += (int64_t)gridDim.x * blockDim.x) {
     int64_t row = t / words_per_row;
@@ -139,13 +149,13 @@ __global__ void packed_phase_kernel(const PackedArgs a, int color) {
       b1 ^= c0;
       b2 |= c1;
     }
-    PackedDecisions dd = D[t];
+    const uint64_t hi = D.hi[t], lo = D.lo[t];
     uint64_t ge3 = b2 | (b1 & b0);                 // e0 >= 3: downhill or level
-    uint64_t e2 = ~b2 & b1 & ~b0;                  // dE = 2
-    uint64_t e1 = ~b2 & ~b1 & b0;                  // dE = 4
-    uint64_t e0z = ~b2 & ~b1 & ~b0;                // dE = 6
-    uint64_t accept = ge3 | (e2 & dd.a2) | (e1 & dd.a4) | (e0z & dd.a6);
-    uint64_t flip = (dd.prop ^ s) & cmask & accept;
+    uint64_t e2 = ~b2 & b1 & ~b0;                  // dE = 2: y < t2
+    uint64_t e1 = ~b2 & ~b1 & b0;                  // dE = 4: y < t4
+    uint64_t e0z = ~b2 & ~b1 & ~b0;                // dE = 6: y < t6
+    uint64_t accept = ge3 | (e2 & (hi | lo)) | (e1 & hi) | (e0z & hi & lo);
+    uint64_t flip = (D.prop[t] ^ s) & cmask & accept;
     if (flip) W[t] = s ^ flip;
     flips += __popcll(flip);
   }
