@@ -829,9 +829,9 @@ static cudaError_t ens_reset(spkgpu_ensemble *e) {
 
 // Autotuner: times one captured step of each mode on this replica set
 // (after a warm-up step, sites all 1) and keeps the faster; the choice is
-// cached per (app, replicas, tiles, exchange period) for the process.
-// SPKGPU_ENSEMBLE_MODE=persistent|launches|launches2|launches4|warps forces a
-// mode (warps only for Ising).
+// cached per (device, app, replicas, tiles, exchange period) for the process.
+// SPKGPU_ENSEMBLE_MODE=persistent|launches|launches2|launches4|warps|warps2|warps4
+// forces a mode (the warp forms only for Ising).
 static const char *const kModeNames[SPKGPU_ENSEMBLE_NMODES] = {"persistent", "launches", "launches2", "launches4",
                                                                 "warps", "warps2", "warps4"};
 
