@@ -128,6 +128,9 @@ ROW_CASES = [
     dict(lattice="sq/8n", nx=18, ny=8, nz=1, app="potts", nspins=5, temperature=0.8, sb=1),
     dict(lattice="sq/8n", nx=32, ny=8, nz=1, app="ising", nspins=2, temperature=1.5, sb=2),
     dict(lattice="sq/8n", nx=64, ny=4, nz=1, app="potts/neigh", nspins=30, temperature=0.4, sb=1),
+    # the largest stamp table (128 value rows of 512 threads) beside 9 int32 rows: opt-in shared memory
+    dict(lattice="sc/26n", nx=1024, ny=4, nz=4, app="potts/neighonly", nspins=127, temperature=0.6, sb=4),
+    dict(lattice="sc/26n", nx=512, ny=6, nz=4, app="potts/neigh", nspins=127, temperature=0.9, sb=1),
 ]
 
 
