@@ -771,7 +771,6 @@ static void ens_capture(spkgpu_ensemble *e) {
     cudaGetLastError();
     return;
   }
-  int64_t nk = 0;
   // external event nodes around the sweep kernels time them in every replay
   bool kev = cudaEventRecordWithFlags(e->kev0, cap, cudaEventRecordExternal) == cudaSuccess;
   cudaError_t le;
@@ -789,7 +788,6 @@ static void ens_capture(spkgpu_ensemble *e) {
       ensemble_bonds_kernel<<<(nt + kBondWarps - 1) / kBondWarps, 32 * kBondWarps, 0, cap>>>(a, e->chunk);
     ensemble_advance_kernel<<<1, 256, 0, cap>>>(a, e->chunk, exchange ? 1 : 0);
     le = cudaGetLastError();
-    (void)nk;
   }
   cudaGraph_t g = nullptr;
   cudaError_t ce = cudaStreamEndCapture(cap, &g);

@@ -325,7 +325,6 @@ bool rows_supported(int lattice, int spin_bytes, int nx, int nspins) {
 
 template <typename S, int LAT, int APP>
 static cudaError_t launch_rows_app(const RowArgs &a, bool smallq, cudaStream_t st) {
-  constexpr int NROWS = Stencil<LAT>::k3d ? 9 : 3;
   int rows_y = (a.ny - a.qy + 1) / 2;
   int rows_z = Stencil<LAT>::k3d ? (a.nz - a.qz + 1) / 2 : 1;
   unsigned grid = (unsigned)(rows_y * rows_z);
